@@ -1,0 +1,406 @@
+"""Benchmark of the LBVH build + closest-hit trace hot path on one GB300.
+
+Workload (one step = one frame): the 1,048,576-triangle fBm terrain (1024 x
+512 quads over [-1,1]^2, 30-bit Morton codes), a 1920x1080 pinhole view from
+(0, 0.6, 1.6), all primary rays traced closest-hit (child-is order), one
+cosine-weighted diffuse bounce ray generated per hit and traced.  The LBVH is
+built once before the timed steps (as the reference builds it in
+create_rt_set and times only traces, rta/main.cpp:402-405); its build is timed
+separately in the same run and reported under "build".
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value  = rays traced per second over the frame's kernels (device-resident rays)
+e2e    = the same frame through the C ABI with host rays: pinned host -> device
+         copy of the primary rays, the frame, device -> host copy of all hits
+N > 1  = independent replicas, one per GPU (weak scaling); the time is the max
+         over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s closest-hit (LBVH terrain, 1920x1080 primary + 1 diffuse bounce)"
+UNIT = "Mrays/s"
+WORKLOAD = "terrain-1M-tris 1024x512 quads, 1920x1080 primary + 1 diffuse bounce, 30-bit Morton, CIS closest hit"
+SEED = 0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--cpu-sample-rays", type=int, default=262144)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# --------------------------------------------------------------------------- #
+# CPU baseline: the reference CPU plugin's algorithm (bbvh spatial-median      #
+# build + child-is tracer, OpenMP), timed on this machine's host cores.       #
+# --------------------------------------------------------------------------- #
+
+def cpu_baseline(tris, orig, dirs, maxt, sample, threads=0):
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    nodes, leaf_tris = O.bbvh_build(tris)
+    build_s = time.perf_counter() - t0
+    n = maxt.shape[0]
+    idx = np.linspace(0, n - 1, min(sample, n)).astype(np.int64)
+    o = orig.reshape(-1, 3)[idx]
+    d = dirs.reshape(-1, 3)[idx]
+    m = maxt[idx]
+    t0 = time.perf_counter()
+    O.bbvh_trace_cis(nodes, leaf_tris, o, d, m, threads=threads)
+    trace_s = time.perf_counter() - t0
+    cores = threads or os.cpu_count()
+    return {"rays": int(idx.shape[0]), "trace_s": trace_s, "build_s": build_s,
+            "mrays_s": idx.shape[0] / trace_s / 1e6, "cores": cores}
+
+
+def run_reference(args):
+    """--impl reference: the reference CPU plugin's build + child-is trace
+    (bbvh/bbvh.h) on the host cores, on a bounded sample of the frame."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from rta_gb300 import scenes as S
+    tris = S.terrain(1024, 512, seed=SEED)
+    cam = S.terrain_camera()
+    o, d, m = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
+    # bounce rays of the frame come from the oracle's restatement of the bounce
+    lb = O.lbvh_build(tris, 30)
+    srt = O.permute(tris, lb.ids)
+    hits, _, _ = O.trace(lb.nodes, srt, o, d, m, O.CIS, 64)
+    bo, bd, bm, _ = O.diffuse_bounce(srt, o, d, hits, seed=SEED, eps=1e-4)
+    allo = np.concatenate([o.reshape(-1, 3), bo.reshape(-1, 3)])
+    alld = np.concatenate([d.reshape(-1, 3), bd.reshape(-1, 3)])
+    allm = np.concatenate([m, bm])
+    t0 = time.perf_counter()
+    nodes, leaf_tris = O.bbvh_build(tris)
+    build_s = time.perf_counter() - t0
+    sample = min(args.cpu_sample_rays, allm.shape[0])
+    idx = np.linspace(0, allm.shape[0] - 1, sample).astype(np.int64)
+    so, sd, sm = allo[idx], alld[idx], allm[idx]
+    for _ in range(args.warmup):
+        O.bbvh_trace_cis(nodes, leaf_tris, so, sd, sm)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.bbvh_trace_cis(nodes, leaf_tris, so, sd, sm)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = sample * args.steps / total / 1e6
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "cpu_sample_rays": sample,
+                                        "cpu_build_s": build_s},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{sample} rays evenly strided over the frame's primary+bounce rays; "
+                                   f"spatial-median bbvh (bbvh/bbvh.h) built once ({build_s:.2f} s)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- #
+# GB300 arm                                                                   #
+# --------------------------------------------------------------------------- #
+
+def run_gb300(args):
+    import torch
+
+    from rta_gb300 import lib as L
+    from rta_gb300 import plugin as P
+    from rta_gb300 import scenes as S
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+
+    lib = L.load()
+    tris = S.terrain(1024, 512, seed=SEED)
+    n = tris.shape[0]
+    cam = S.terrain_camera()
+    nrays = cam.w * cam.h
+    ftl = P.cuda_ftl(tris)
+    ctor = P.lbvh_constructor(morton_bits=30, keep_triangles=False)
+    stream = torch.cuda.current_stream()
+    sh = L.stream_handle(stream)
+
+    # L2 flush buffer (larger than the 129 MB L2)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    # ---- build timing ----
+    for _ in range(args.warmup):
+        bvh = ctor.build(ftl)
+    build_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        L.check(lib.rta_lbvh_build(ctor.handle, P._ptr(ftl.triangle), n, 30, C.c_void_p(0), sh), "build")
+        e1.record()
+        e1.synchronize()
+        build_ms.append(e0.elapsed_time(e1))
+    bvh = P.binary_lbvh(ctor, None)
+    assert bvh.status() & (L.DEV_SPIN_TIMEOUT | L.DEV_STACK_OVERFLOW) == 0
+
+    # ---- rays, frame context ----
+    rg = P.cam_ray_generator_shirley(cam.w, cam.h)
+    rg.setup(cam.pos, cam.dir, cam.up, cam.fovy)
+    rg.generate_rays()
+    hits = torch.empty(nrays * 4, dtype=torch.float32, device=dev)
+    fh = C.c_void_p()
+    L.check(lib.rta_frame_create(C.byref(fh), nrays), "rta_frame_create")
+    frame = L.FrameView()
+    L.check(lib.rta_frame_get(fh, C.byref(frame)), "rta_frame_get")
+    count_view = P.device_view(frame.count, 1, "<u4")
+
+    def run_frame():
+        L.check(lib.rta_frame_run(fh, C.byref(bvh.view), P._ptr(rg.gpu_origin), P._ptr(rg.gpu_direction),
+                                  P._ptr(rg.gpu_maxt), nrays, P._ptr(hits), L.TRACE_CIS, SEED,
+                                  np.float32(1e-4), sh), "rta_frame_run")
+
+    for _ in range(args.warmup):
+        run_frame()
+    torch.cuda.synchronize()
+    nbounce = int(count_view.cpu().numpy().view(np.uint32)[0])
+    rays_per_step = nrays + nbounce
+
+    # per-ray work counts (one stats pass, outside the timed region)
+    st = torch.zeros(2 * nrays, dtype=torch.int32, device=dev)
+    tmp = torch.empty_like(hits)
+    L.check(lib.rta_trace(C.byref(bvh.view), P._ptr(rg.gpu_origin), P._ptr(rg.gpu_direction),
+                          P._ptr(rg.gpu_maxt), nrays, C.c_void_p(0), P._ptr(tmp),
+                          L.TRACE_CIS | L.TRACE_STATS, P._ptr(st), sh), "stats")
+    stp = st.view(-1, 2).to(torch.int64).sum(0).cpu().numpy()
+    stb = torch.zeros(2 * nrays, dtype=torch.int32, device=dev)
+    L.check(lib.rta_trace(C.byref(bvh.view), C.c_void_p(frame.orig), C.c_void_p(frame.dir),
+                          C.c_void_p(frame.maxt), 0, C.c_void_p(frame.count), P._ptr(tmp),
+                          L.TRACE_CIS | L.TRACE_STATS, P._ptr(stb), sh), "stats")
+    stbs = stb.view(-1, 2).to(torch.int64).sum(0).cpu().numpy()
+    inner_visits = int(stp[0] + stbs[0])
+    tri_tests = int(stp[1] + stbs[1])
+
+    # ---- timed frames (device-resident rays) ----
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    step_ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            run_frame()
+            e1.record()
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        # primary trace kernel alone: the roofline kernel
+        trace_ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            L.check(lib.rta_trace(C.byref(bvh.view), P._ptr(rg.gpu_origin), P._ptr(rg.gpu_direction),
+                                  P._ptr(rg.gpu_maxt), nrays, C.c_void_p(0), P._ptr(tmp), L.TRACE_CIS,
+                                  C.c_void_p(0), sh), "trace")
+            e1.record()
+            e1.synchronize()
+            trace_ms.append(e0.elapsed_time(e1))
+    if pg:
+        pg.barrier()
+    total_ms = sum(step_ms)
+    if pg:
+        t = torch.tensor([total_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = rays_per_step * world * args.steps / (total_ms * 1e-3) / 1e6
+
+    # ---- e2e: host rays in, host hits out, through the C ABI ----
+    h_orig = torch.empty(3 * nrays, dtype=torch.float32, pin_memory=True)
+    h_dir = torch.empty(3 * nrays, dtype=torch.float32, pin_memory=True)
+    h_maxt = torch.empty(nrays, dtype=torch.float32, pin_memory=True)
+    h_orig.copy_(rg.gpu_origin)
+    h_dir.copy_(rg.gpu_direction)
+    h_maxt.copy_(rg.gpu_maxt)
+    h_hits = torch.empty(nrays * 4, dtype=torch.float32, pin_memory=True)
+    h_bhits = torch.empty(nrays * 4, dtype=torch.float32, pin_memory=True)
+    d_orig, d_dir, d_maxt = torch.empty_like(rg.gpu_origin), torch.empty_like(rg.gpu_direction), torch.empty_like(rg.gpu_maxt)
+    bhits_view = P.device_view(frame.hits, 4 * nrays)
+
+    def e2e_step():
+        d_orig.copy_(h_orig, non_blocking=True)
+        d_dir.copy_(h_dir, non_blocking=True)
+        d_maxt.copy_(h_maxt, non_blocking=True)
+        L.check(lib.rta_frame_run(fh, C.byref(bvh.view), P._ptr(d_orig), P._ptr(d_dir), P._ptr(d_maxt),
+                                  nrays, P._ptr(hits), L.TRACE_CIS, SEED, np.float32(1e-4), sh), "frame")
+        h_hits.copy_(hits, non_blocking=True)
+        h_bhits[: 4 * nbounce].copy_(bhits_view[: 4 * nbounce], non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record()
+    e1.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    h2d = (3 + 3 + 1) * 4 * nrays
+    d2h = 16 * nrays + 16 * nbounce
+    e2e_value = rays_per_step * world / (e2e_ms * 1e-3) / 1e6
+
+    # ---- roofline of the primary trace kernel ----
+    peak, peak_kind = measured_peaks()
+    tr_ms = statistics.mean(trace_ms)
+    bytes_per_launch = 28 * nrays + 16 * nrays + 64 * int(stp[0]) + 48 * int(stp[1])
+    achieved = bytes_per_launch / (tr_ms * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "trace_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu_r = cpu_baseline(tris, rg.gpu_origin.cpu().numpy(), rg.gpu_direction.cpu().numpy(),
+                             rg.gpu_maxt.cpu().numpy(), args.cpu_sample_rays)
+        cpu = {"value": cpu_r["mrays_s"], "unit": UNIT, "cores": cpu_r["cores"], "kind": "port",
+               "sample": f"{cpu_r['rays']} primary rays evenly strided over the 1920x1080 frame through "
+                         f"the spatial-median bbvh of the same terrain (build {cpu_r['build_s']:.2f} s, untimed)"}
+
+    bmean = statistics.mean(build_ms)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "triangles": n, "primary_rays": nrays, "bounce_rays": nbounce,
+                   "rays_per_step": rays_per_step, "morton_bits": 30,
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_trace<CIS> primary 1920x1080",
+                     "algorithmic_bytes_per_launch": bytes_per_launch, "kernel_ms": tr_ms,
+                     "peak_source": peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms},
+        "gpu_launches": 5 * args.steps,
+        "clocks": clk.summary(),
+        "build": {"ms": bmean, "ms_min": min(build_ms), "mtri_s": n / (bmean * 1e-3) / 1e6,
+                  "algorithmic_bytes": 372 * n, "achieved_gbs": 372 * n / (bmean * 1e-3) / 1e9,
+                  "frac_of_peak": 372 * n / (bmean * 1e-3) / 1e9 / peak},
+        "trace": {"primary_ms": tr_ms, "primary_mrays_s": nrays / (tr_ms * 1e-3) / 1e6,
+                  "inner_visits_per_ray": inner_visits / rays_per_step,
+                  "tri_tests_per_ray": tri_tests / rays_per_step},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    L.check(lib.rta_frame_destroy(fh), "rta_frame_destroy")
+    if pg:
+        pg.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,183 @@
+/*
+ * rta_gb300.h -- C ABI of the GB300 LBVH builder and binary-BVH tracer.
+ *
+ * Plain C: device pointers, sizes and a CUDA stream; every call returns an
+ * int status (RTA_OK or a negative RTA_ERR_*), never exits the process.  The
+ * rta plugin (plugin/bbvh_gb300.cpp) converts a failure into the reference's
+ * behaviour (print and exit, librta/cuda.h:70-77) at the plugin boundary.
+ *
+ * Each entry point names the reference function it replaces (kiselgra/rta,
+ * path:line).  Host-visible layouts that cross this boundary are the
+ * reference's:
+ *   triangles  cuda::simple_triangle, 104 bytes (librta/cuda-vec.h:30-37),
+ *              positions a,b,c at byte offsets 0..35
+ *   rays       origin float[3*n], direction float[3*n], max_t float[n]
+ *              (librta/cuda.h:90-107)
+ *   hits       triangle_intersection {float t, beta, gamma; uint ref},
+ *              16 bytes (librta/basic_types.h:81-95); ref indexes the
+ *              Morton-ordered triangle array, miss <=> t == FLT_MAX
+ *   2F4 nodes  bbvh_node_float4 (bbvh-cuda/bbvh-cuda-node.h:37-91), only
+ *              produced on request for dumps and parity checks
+ */
+#ifndef RTA_GB300_H
+#define RTA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *rta_stream_t; /* a cudaStream_t; NULL = legacy default stream */
+
+/* ---- status codes ---- */
+#define RTA_OK 0
+#define RTA_ERR_INVALID (-1)     /* bad argument (null pointer, n == 0, size limit) */
+#define RTA_ERR_CUDA (-2)        /* a CUDA runtime call failed; see rta_last_error() */
+#define RTA_ERR_DEVICE (-3)      /* a kernel raised a device status flag */
+#define RTA_ERR_NOMEM (-4)       /* device allocation failed */
+
+/* device status flags (rta_lbvh_status, rta_frame_status) */
+#define RTA_DEV_STACK_OVERFLOW 1u  /* a ray's traversal stack overflowed; that ray is unfinished */
+#define RTA_DEV_SPIN_TIMEOUT 2u    /* a bounded wait in a single-pass scan gave up */
+#define RTA_DEV_QUANT_WRAP 4u      /* a quantised centroid reached the grid size and wrapped (reference quirk, kept) */
+#define RTA_DEV_ZERO_EXTENT 8u     /* a scene axis has zero extent (scale is inf, reference quirk, kept) */
+#define RTA_DEV_ITER_LIMIT 16u     /* a traversal or refit loop hit its iteration cap and stopped */
+#define RTA_DEV_BAD_LINK 32u       /* a node link or triangle index was out of range; the access was skipped */
+
+/* trace modes: rta plugin flags -t dis|cis, -s, -A (bbvh-cuda/main.cpp:40-51) */
+#define RTA_TRACE_CIS 0u     /* child-is closest hit (kernels.cu:777-855) */
+#define RTA_TRACE_DIS 1u     /* direct-is (kernels.cu:486-548) */
+#define RTA_TRACE_SHADOW 2u  /* any hit: stop at the first accepted hit (kernels.cu:857-939) */
+#define RTA_TRACE_AILA 4u    /* Aila-Laine reciprocal box test (intersect.h:165-176) */
+#define RTA_TRACE_STATS 8u   /* also write per-ray counts {inner nodes visited, triangles tested} */
+
+/* Message of the last failing CUDA call in this thread ("" if none). */
+const char *rta_last_error(void);
+
+/* Largest triangle count one LBVH may hold (leaf links carry 25-bit offsets). */
+uint32_t rta_lbvh_max_triangles(void);
+
+/* ------------------------------------------------------------------------ */
+/* LBVH construction -- replaces lbvh_constructor (bbvh-cuda/lbvh.h:49-216)  */
+/* ------------------------------------------------------------------------ */
+
+typedef struct rta_lbvh_ctx rta_lbvh_ctx;
+
+/* Device view of a built LBVH.  All pointers are device pointers owned by
+ * the context; they stay valid until the next build or reserve. */
+typedef struct rta_lbvh {
+    const void *nodes;       /* (n-1) inner-node records, 64 bytes each */
+    const void *root;        /* root record, 32 bytes: box min xyz, max xyz, link, pad */
+    const void *tris;        /* n Morton-ordered triangles, 48 bytes each */
+    const uint32_t *index;   /* n: Morton position -> input triangle id (lbvh.h:20-28) */
+    const void *codes;       /* n sorted Morton codes: uint32 (30-bit) or uint64 (63-bit) */
+    const uint32_t *parents; /* 2n-1 parent links ((parent << 1) | side), reference numbering */
+    uint32_t n;
+    int32_t morton_bits;
+    uint32_t *status;        /* device word of RTA_DEV_* flags */
+} rta_lbvh;
+
+/* new/delete of lbvh_constructor (lbvh.h:114-145) */
+int rta_lbvh_create(rta_lbvh_ctx **ctx);
+int rta_lbvh_destroy(rta_lbvh_ctx *ctx);
+
+/* setupCudaMemory (lbvh-kernels.cu:368-383): sizes the device buffers for up to
+ * n triangles; build() calls it when n grows, as buildCUDA does (lbvh.h:157-162). */
+int rta_lbvh_reserve(rta_lbvh_ctx *ctx, uint32_t n, int morton_bits);
+
+/* lbvh_constructor::buildCUDA (lbvh.h:153-211): initTriangles,
+ * calculateVoxelBounds, calculateMortonCodes2, sortMortonCodes,
+ * buildTreeKarras, buildBoundingBoxesKarras2, invert_triangle_permutation_cuda
+ * (lbvh-kernels.cu:405-578), as one stream-ordered sequence with no host sync.
+ *   tris       n input triangles (device, 104 bytes each); not modified
+ *   morton_bits 30 (the reference's 10 bits per axis) or 63 (21 bits per axis)
+ *   tris_out   optional (nullable): receives the input records gathered into
+ *              Morton order, the array the reference writes back into its
+ *              input buffer and indexes with triangle_intersection::ref */
+int rta_lbvh_build(rta_lbvh_ctx *ctx, const void *tris, uint32_t n, int morton_bits,
+                   void *tris_out, rta_stream_t stream);
+
+/* the built tree: binary_lbvh::take_node_array / take_index_array (lbvh.h:207-208) */
+int rta_lbvh_get(const rta_lbvh_ctx *ctx, rta_lbvh *out);
+
+/* Synchronises the stream and returns the device status flags (RTA_DEV_*). */
+int rta_lbvh_status(const rta_lbvh *bvh, rta_stream_t stream, uint32_t *flags);
+
+/* Writes the tree in the reference's 2F4 node layout ((2n-1) x 32 bytes),
+ * node for node as buildTreeKarras + buildBoundingBoxesKarras2 leave it, for
+ * dumps (bbvh.h:36-52) and parity checks. */
+int rta_lbvh_to_2f4(const rta_lbvh *bvh, void *nodes_2f4, rta_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* traversal -- replaces trace_cis / trace_dis / trace_shadow_* / *_ailabox  */
+/* (bbvh-cuda/kernels.cu:1145-1338, host launchers)                          */
+/* ------------------------------------------------------------------------ */
+
+/* Traces nrays rays (or *d_nrays if d_nrays is not NULL, read on the device)
+ * through bvh.  hits: nrays records; a hit overwrites the record, a miss
+ * writes only t = FLT_MAX (the reference keeps beta/gamma/ref of the
+ * record, kernels.cu:794-796).  stats: optional, 2 uint32 per ray when
+ * RTA_TRACE_STATS is set.  Rays are fetched in warp batches from a global
+ * queue by a persistent grid. */
+int rta_trace(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt,
+              uint32_t nrays, const uint32_t *d_nrays, void *hits, uint32_t mode,
+              uint32_t *stats, rta_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* rays -- librta/cuda-kernels.cu                                            */
+/* ------------------------------------------------------------------------ */
+
+/* setup_shirley_rays (cuda-kernels.cu:50-112).  tan_half_fovy is the value the
+ * reference kernel computes as tanf(M_PI*(fovy/2)/180.0f); the caller passes
+ * it (cuda::cam_ray_generator_shirley computes it once per frame). */
+int rta_setup_shirley_rays(float *dirs, float *orgs, float *maxts, float tan_half_fovy,
+                           float aspect, int w, int h, const float view_dir[3],
+                           const float pos[3], const float up[3], float maxt,
+                           rta_stream_t stream);
+
+/* reset_intersections (cuda-kernels.cu:24-44): t = FLT_MAX, beta = 1, gamma = 2. */
+int rta_reset_intersections(void *hits, uint32_t w, uint32_t h, rta_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* frame: primary trace + one diffuse bounce (no reference counterpart: the  */
+/* reference's cuda bouncers never trace further, cuda.h:208-220)            */
+/* ------------------------------------------------------------------------ */
+
+typedef struct rta_frame_ctx rta_frame_ctx;
+
+/* Device view of a frame's bounce pass. */
+typedef struct rta_frame {
+    float *orig, *dir, *maxt;  /* bounce rays, compacted in primary ray order */
+    uint32_t *src;             /* primary ray index of each bounce ray */
+    void *hits;                /* bounce hits, 16 bytes each */
+    uint32_t *count;           /* device: number of bounce rays */
+    uint32_t capacity;
+} rta_frame;
+
+int rta_frame_create(rta_frame_ctx **ctx, uint32_t max_rays);
+int rta_frame_destroy(rta_frame_ctx *ctx);
+int rta_frame_get(const rta_frame_ctx *ctx, rta_frame *out);
+
+/* One cosine-weighted diffuse bounce ray per primary hit, compacted in ray
+ * order by a single-pass scan: origin = hit point pushed eps along the
+ * geometric normal (facing the incoming ray), direction from the seeded
+ * uniform pair (seed, 2i) and (seed, 2i+1), max_t = FLT_MAX. */
+int rta_diffuse_bounce(rta_frame_ctx *ctx, const rta_lbvh *bvh, const float *orig,
+                       const float *dir, const void *hits, uint32_t nrays, uint32_t seed,
+                       float eps, rta_stream_t stream);
+
+/* Whole frame: reset primary hits, trace primary rays, generate the bounce,
+ * reset bounce hits, trace the bounce rays.  No host synchronisation. */
+int rta_frame_run(rta_frame_ctx *ctx, const rta_lbvh *bvh, const float *orig, const float *dir,
+                  const float *maxt, uint32_t nrays, void *hits, uint32_t mode, uint32_t seed,
+                  float eps, rta_stream_t stream);
+
+/* Synchronises and returns the frame's device status flags. */
+int rta_frame_status(rta_frame_ctx *ctx, rta_stream_t stream, uint32_t *flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

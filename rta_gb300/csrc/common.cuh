@@ -1,0 +1,132 @@
+// common.cuh -- device layouts and helpers shared by the LBVH build, the
+// traversal and the ray kernels (sm_103a).
+//
+// Device layouts (all 16-byte aligned, sized for vector loads):
+//   NodeRec  64 B per inner node i in [0, n-2] (the reference numbers inner
+//            nodes 0..n-2 and leaves n-1..2n-2, lbvh-kernels.cu:197-203).  A
+//            node stores the boxes and links of BOTH children, so the
+//            child-is test of an inner node is one 64-byte fetch:
+//              q0 = left  (lo.x, hi.x, lo.y, hi.y)
+//              q1 = left  (lo.z, hi.z), right (lo.x, hi.x)
+//              q2 = right (lo.y, hi.y, lo.z, hi.z)
+//              q3 = (left link, right link, left ref-index, right ref-index)
+//            The ref-index words keep the reference's node numbering of the
+//            children so the tree can be written out in its 2F4 layout.
+//   RootRec  32 B: root box and root link.
+//   TriRec   48 B per triangle in Morton order: (a, count), (b, id), (c, 0).
+//            count = number of triangles of the leaf that starts here.
+//   link     bit 31 clear: inner node index.  Bit 31 set: a leaf,
+//            bits 30..25 = min(count, 64) - 1 (63 = look up count in the
+//            TriRec), bits 24..0 = first triangle (Morton position).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+
+#include "../../include/rta_gb300.h"
+
+namespace rta {
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr uint32_t kCountShift = 25;
+constexpr uint32_t kCountMask = 0x3fu;
+constexpr uint32_t kFirstMask = (1u << kCountShift) - 1u;
+constexpr uint32_t kMaxTriangles = 1u << kCountShift;
+
+struct __align__(16) NodeRec {
+    float4 q0, q1, q2;
+    uint4 q3;
+};
+static_assert(sizeof(NodeRec) == 64, "node record");
+
+struct __align__(16) RootRec {
+    float lo[3], hi[3];
+    uint32_t link, pad;
+};
+static_assert(sizeof(RootRec) == 32, "root record");
+
+struct __align__(16) TriRec {
+    float4 v0, v1, v2;
+};
+static_assert(sizeof(TriRec) == 48, "triangle record");
+
+struct HitRec {
+    float t, beta, gamma;
+    uint32_t ref;
+};
+
+__host__ __device__ __forceinline__ bool is_leaf(uint32_t link) { return (link & kLeafBit) != 0u; }
+__host__ __device__ __forceinline__ uint32_t leaf_first(uint32_t link) { return link & kFirstMask; }
+__host__ __device__ __forceinline__ uint32_t leaf_count_field(uint32_t link)
+{
+    return (link >> kCountShift) & kCountMask;
+}
+__host__ __device__ __forceinline__ uint32_t make_leaf(uint32_t first, uint32_t count)
+{
+    uint32_t f = count >= 64u ? 63u : count - 1u;
+    return kLeafBit | (f << kCountShift) | first;
+}
+
+// The reference's MIN / MAX macros (lbvh-kernels.cu:142-143): ternaries, not
+// fminf/fmaxf, so that equal-valued signed zeros resolve the same way.
+__host__ __device__ __forceinline__ float ref_min(float a, float b) { return (a < b) ? a : b; }
+__host__ __device__ __forceinline__ float ref_max(float a, float b) { return (a > b) ? a : b; }
+
+// Bounded spin: every wait on another block gives up after this many polls
+// and raises RTA_DEV_SPIN_TIMEOUT instead of hanging the GPU.
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p)
+{
+    return *(const volatile uint32_t *)p;
+}
+__device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v) { *(volatile uint32_t *)p = v; }
+
+// decoupled look-back status words: 2 flag bits + 30-bit value
+constexpr uint32_t kStatAggregate = 1u << 30;
+constexpr uint32_t kStatPrefix = 2u << 30;
+constexpr uint32_t kStatValue = (1u << 30) - 1u;
+
+// Walks tile statuses backwards from tile-1 until an inclusive prefix is found;
+// returns the exclusive prefix of `tile` for one counter.  stat[t * stride]
+// is tile t's word.  Bounded: sets RTA_DEV_SPIN_TIMEOUT in *flags on give-up.
+__device__ __forceinline__ uint32_t lookback(const uint32_t *stat, uint32_t stride, uint32_t tile,
+                                             uint32_t *flags)
+{
+    uint32_t excl = 0;
+    int t = (int)tile - 1;
+    uint32_t spins = 0;
+    while (t >= 0) {
+        uint32_t s = ld_volatile(stat + (size_t)t * stride);
+        if ((s & ~kStatValue) == 0u) {
+            if (++spins > kSpinLimit) {
+                atomicOr(flags, RTA_DEV_SPIN_TIMEOUT);
+                break;
+            }
+            __nanosleep(32);
+            continue;
+        }
+        excl += s & kStatValue;
+        if (s & kStatPrefix) break;
+        --t;
+    }
+    return excl;
+}
+
+} // namespace rta
+
+// host-side error helpers (one translation unit defines the storage)
+namespace rta {
+void set_cuda_error(cudaError_t e, const char *where);
+int check_launch(const char *where);
+}
+
+#define RTA_CUDA_TRY(call)                                                                   \
+    do {                                                                                     \
+        cudaError_t _e = (call);                                                             \
+        if (_e != cudaSuccess) {                                                             \
+            rta::set_cuda_error(_e, #call);                                                  \
+            return _e == cudaErrorMemoryAllocation ? RTA_ERR_NOMEM : RTA_ERR_CUDA;           \
+        }                                                                                    \
+    } while (0)

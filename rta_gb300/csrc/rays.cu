@@ -1,0 +1,381 @@
+// rays.cu -- camera rays, intersection reset and the diffuse bounce pass.
+//
+//   k_shirley   setup_shirley_rays (librta/cuda-kernels.cu:50-112), the
+//               reference's arithmetic through explicit IEEE intrinsics
+//   k_reset     reset_intersections (librta/cuda-kernels.cu:24-44)
+//   k_bounce    one cosine-weighted diffuse bounce ray per hit (no reference
+//               counterpart), compacted in primary-ray order by a single-pass
+//               scan with decoupled look-back
+#include "common.cuh"
+
+namespace rta {
+
+int trace_impl(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt,
+               uint32_t nrays, const uint32_t *d_nrays, void *hits, uint32_t mode, uint32_t *stats,
+               uint32_t *queue, cudaStream_t s);
+
+// librta/cuda-vec.h:157-193 in the same operation order
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 v_div(V3 a, float s)
+{
+    return {__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s)};
+}
+__device__ __forceinline__ V3 v_mul(V3 a, float s)
+{
+    return {__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s)};
+}
+__device__ __forceinline__ V3 v_add(V3 a, V3 b)
+{
+    return {__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)};
+}
+__device__ __forceinline__ float v_dot(V3 a, V3 b)
+{
+    float s = __fmul_rn(a.x, b.x);
+    s = __fadd_rn(s, __fmul_rn(a.y, b.y));
+    s = __fadd_rn(s, __fmul_rn(a.z, b.z));
+    return s;
+}
+__device__ __forceinline__ float v_len(V3 a) { return __fsqrt_rn(v_dot(a, a)); }
+__device__ __forceinline__ V3 v_cross(V3 l, V3 r)
+{
+    return {__fsub_rn(__fmul_rn(l.y, r.z), __fmul_rn(l.z, r.y)),
+            __fsub_rn(__fmul_rn(l.z, r.x), __fmul_rn(l.x, r.z)),
+            __fsub_rn(__fmul_rn(l.x, r.y), __fmul_rn(l.y, r.x))};
+}
+
+__global__ void k_shirley(float *__restrict__ dirs, float *__restrict__ orgs, float *__restrict__ maxts,
+                          float height, float aspect, int w, int h, V3 vd, V3 pos, V3 up, float maxt)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const size_t id = (size_t)y * w + x;
+    orgs[3 * id + 0] = pos.x;
+    orgs[3 * id + 1] = pos.y;
+    orgs[3 * id + 2] = pos.z;
+    maxts[id] = maxt;
+    const float width = __fmul_rn(aspect, height);
+    float u_s = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn((float)x, 0.5f), (float)w), 2.0f), 1.0f);
+    float v_s = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn((float)y, 0.5f), (float)h), 2.0f), 1.0f);
+    u_s = __fmul_rn(width, u_s);
+    v_s = __fmul_rn(height, v_s);
+    V3 W = v_div(vd, v_len(vd));
+    V3 TxW = v_cross(up, W);
+    V3 U = v_div(TxW, v_len(TxW));
+    V3 V = v_cross(W, U);
+    V3 dir = v_mul(U, u_s);
+    V3 tmp = v_mul(V, v_s);
+    dir = v_add(dir, tmp);
+    dir = v_add(dir, W);
+    dir = v_div(dir, v_len(dir));
+    dirs[3 * id + 0] = dir.x;
+    dirs[3 * id + 1] = dir.y;
+    dirs[3 * id + 2] = dir.z;
+}
+
+__global__ void k_reset(HitRec *__restrict__ hits, uint32_t n, const uint32_t *__restrict__ d_n)
+{
+    const uint32_t cnt = d_n ? *d_n : n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+        hits[i].t = FLT_MAX;
+        hits[i].beta = 1.0f;
+        hits[i].gamma = 2.0f;
+    }
+}
+
+// ---- diffuse bounce ---- //
+
+// 32-bit xor-shift-multiply finaliser; the oracle uses the same function
+__device__ __forceinline__ uint32_t hash32(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+__device__ __forceinline__ float uniform01(uint32_t seed, uint32_t index)
+{
+    uint32_t h = hash32(index * 0x9e3779b1u + hash32(seed ^ 0x5bd1e995u));
+    return __fmul_rn((float)(h >> 8), 1.0f / 16777216.0f);
+}
+
+// cos and sin of 2*pi*u: quarter-turn reduction and Taylor polynomials in
+// Horner form with fused multiply-adds -- IEEE operations only, so the
+// oracle reproduces them bit for bit
+__device__ __forceinline__ void cos_sin_2pi(float u, float &c, float &s)
+{
+    float u4 = __fmul_rn(u, 4.0f);
+    int q = (int)u4;
+    if (q > 3) q = 3;
+    float f = __fsub_rn(u4, (float)q);
+    float th = __fmul_rn(f, 1.57079637f);
+    float x2 = __fmul_rn(th, th);
+    float sp = -2.50521084e-08f;
+    sp = __fmaf_rn(sp, x2, 2.75573192e-06f);
+    sp = __fmaf_rn(sp, x2, -1.98412698e-04f);
+    sp = __fmaf_rn(sp, x2, 8.33333333e-03f);
+    sp = __fmaf_rn(sp, x2, -1.66666667e-01f);
+    sp = __fmaf_rn(sp, x2, 1.0f);
+    float sn = __fmul_rn(sp, th);
+    float cp = 2.08767570e-09f;
+    cp = __fmaf_rn(cp, x2, -2.75573192e-07f);
+    cp = __fmaf_rn(cp, x2, 2.48015873e-05f);
+    cp = __fmaf_rn(cp, x2, -1.38888889e-03f);
+    cp = __fmaf_rn(cp, x2, 4.16666667e-02f);
+    cp = __fmaf_rn(cp, x2, -0.5f);
+    float cs = __fmaf_rn(cp, x2, 1.0f);
+    switch (q) {
+    case 0: c = cs; s = sn; break;
+    case 1: c = -sn; s = cs; break;
+    case 2: c = -cs; s = -sn; break;
+    default: c = sn; s = -cs; break;
+    }
+}
+
+constexpr int kBounceThreads = 256;
+constexpr int kBounceItems = 4;
+constexpr int kBounceTile = kBounceThreads * kBounceItems;
+
+struct FrameState {
+    uint32_t tile_ctr;
+    uint32_t count;
+    uint32_t queue;
+    uint32_t status;
+};
+
+__global__ void __launch_bounds__(kBounceThreads)
+k_bounce(const TriRec *__restrict__ tris, const float *__restrict__ orig, const float *__restrict__ dir,
+         const HitRec *__restrict__ hits, uint32_t nrays, uint32_t seed, float eps,
+         float *__restrict__ oo, float *__restrict__ od, float *__restrict__ om,
+         uint32_t *__restrict__ osrc, uint32_t *__restrict__ tstat, FrameState *__restrict__ fs,
+         uint32_t n_tris)
+{
+    __shared__ uint32_t s_tile, s_warp[kBounceThreads / 32], s_base;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(&fs->tile_ctr, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t ntiles = (nrays + kBounceTile - 1) / kBounceTile;
+    // blocked arrangement: thread owns rays base + tid*ITEMS + k (ray order)
+    const uint32_t first = tile * kBounceTile + tid * kBounceItems;
+    bool hit[kBounceItems];
+    uint32_t mine = 0;
+#pragma unroll
+    for (int k = 0; k < kBounceItems; ++k) {
+        uint32_t i = first + k;
+        hit[k] = i < nrays && hits[i].t != FLT_MAX && hits[i].ref < n_tris;
+        mine += hit[k];
+    }
+    // block exclusive scan of per-thread counts
+    uint32_t x = mine;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) s_warp[w] = x;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t run = 0;
+        for (int j = 0; j < kBounceThreads / 32; ++j) {
+            uint32_t c = s_warp[j];
+            s_warp[j] = run;
+            run += c;
+        }
+        // run = tile total; publish and look back
+        uint32_t *my = tstat + tile;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            st_volatile(my, kStatPrefix | run);
+        } else {
+            st_volatile(my, kStatAggregate | run);
+            excl = lookback(tstat, 1, tile, &fs->status);
+            __threadfence();
+            st_volatile(my, kStatPrefix | ((excl + run) & kStatValue));
+        }
+        s_base = excl;
+        if (tile == ntiles - 1) fs->count = excl + run;
+    }
+    __syncthreads();
+    uint32_t pos = s_base + s_warp[w] + x - mine;
+#pragma unroll
+    for (int k = 0; k < kBounceItems; ++k) {
+        if (!hit[k]) continue;
+        const uint32_t i = first + k;
+        const HitRec hr = hits[i];
+        const TriRec T = tris[hr.ref];
+        V3 o = {orig[3 * (size_t)i], orig[3 * (size_t)i + 1], orig[3 * (size_t)i + 2]};
+        V3 d = {dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]};
+        V3 p = {__fadd_rn(o.x, __fmul_rn(hr.t, d.x)), __fadd_rn(o.y, __fmul_rn(hr.t, d.y)),
+                __fadd_rn(o.z, __fmul_rn(hr.t, d.z))};
+        V3 e1 = {__fsub_rn(T.v1.x, T.v0.x), __fsub_rn(T.v1.y, T.v0.y), __fsub_rn(T.v1.z, T.v0.z)};
+        V3 e2 = {__fsub_rn(T.v2.x, T.v0.x), __fsub_rn(T.v2.y, T.v0.y), __fsub_rn(T.v2.z, T.v0.z)};
+        V3 nrm = v_cross(e1, e2);
+        nrm = v_div(nrm, v_len(nrm));
+        if (v_dot(nrm, d) > 0.0f) nrm = {-nrm.x, -nrm.y, -nrm.z};
+        const float u1 = uniform01(seed, 2u * i), u2 = uniform01(seed, 2u * i + 1u);
+        const float rr = __fsqrt_rn(u1);
+        float cs, sn;
+        cos_sin_2pi(u2, cs, sn);
+        const float lx = __fmul_rn(rr, cs), ly = __fmul_rn(rr, sn);
+        const float one_m = __fsub_rn(1.0f, u1);
+        const float lz = __fsqrt_rn(one_m > 0.0f ? one_m : 0.0f);
+        // orthonormal basis: Duff et al., JCGT 6(1), 2017
+        const float sg = copysignf(1.0f, nrm.z);
+        const float a = __fdiv_rn(-1.0f, __fadd_rn(sg, nrm.z));
+        const float b = __fmul_rn(__fmul_rn(nrm.x, nrm.y), a);
+        const V3 b1 = {__fadd_rn(1.0f, __fmul_rn(__fmul_rn(__fmul_rn(sg, nrm.x), nrm.x), a)),
+                       __fmul_rn(sg, b), -__fmul_rn(sg, nrm.x)};
+        const V3 b2 = {b, __fadd_rn(sg, __fmul_rn(__fmul_rn(nrm.y, nrm.y), a)), -nrm.y};
+        const float bx = __fadd_rn(__fadd_rn(__fmul_rn(b1.x, lx), __fmul_rn(b2.x, ly)), __fmul_rn(nrm.x, lz));
+        const float by = __fadd_rn(__fadd_rn(__fmul_rn(b1.y, lx), __fmul_rn(b2.y, ly)), __fmul_rn(nrm.y, lz));
+        const float bz = __fadd_rn(__fadd_rn(__fmul_rn(b1.z, lx), __fmul_rn(b2.z, ly)), __fmul_rn(nrm.z, lz));
+        od[3 * (size_t)pos + 0] = bx;
+        od[3 * (size_t)pos + 1] = by;
+        od[3 * (size_t)pos + 2] = bz;
+        oo[3 * (size_t)pos + 0] = __fadd_rn(p.x, __fmul_rn(nrm.x, eps));
+        oo[3 * (size_t)pos + 1] = __fadd_rn(p.y, __fmul_rn(nrm.y, eps));
+        oo[3 * (size_t)pos + 2] = __fadd_rn(p.z, __fmul_rn(nrm.z, eps));
+        om[pos] = FLT_MAX;
+        osrc[pos] = i;
+        ++pos;
+    }
+}
+
+} // namespace rta
+
+using namespace rta;
+
+struct rta_frame_ctx {
+    uint32_t cap = 0;
+    float *orig = nullptr, *dir = nullptr, *maxt = nullptr;
+    uint32_t *src = nullptr;
+    HitRec *hits = nullptr;
+    uint32_t *tstat = nullptr;
+    FrameState *fs = nullptr;
+};
+
+extern "C" {
+
+int rta_setup_shirley_rays(float *dirs, float *orgs, float *maxts, float tan_half_fovy, float aspect,
+                           int w, int h, const float view_dir[3], const float pos[3],
+                           const float up[3], float maxt, rta_stream_t stream)
+{
+    if (!dirs || !orgs || !maxts || !view_dir || !pos || !up || w <= 0 || h <= 0) return RTA_ERR_INVALID;
+    dim3 threads(16, 16);
+    dim3 blocks((w + 15) / 16, (h + 15) / 16);
+    k_shirley<<<blocks, threads, 0, (cudaStream_t)stream>>>(
+        dirs, orgs, maxts, tan_half_fovy, aspect, w, h, V3{view_dir[0], view_dir[1], view_dir[2]},
+        V3{pos[0], pos[1], pos[2]}, V3{up[0], up[1], up[2]}, maxt);
+    return check_launch("k_shirley");
+}
+
+int rta_reset_intersections(void *hits, uint32_t w, uint32_t h, rta_stream_t stream)
+{
+    if (!hits || w == 0 || h == 0) return RTA_ERR_INVALID;
+    const uint32_t n = w * h;
+    const uint32_t blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+    k_reset<<<blocks, 256, 0, (cudaStream_t)stream>>>((HitRec *)hits, n, nullptr);
+    return check_launch("k_reset");
+}
+
+int rta_frame_create(rta_frame_ctx **out, uint32_t max_rays)
+{
+    if (!out || max_rays == 0) return RTA_ERR_INVALID;
+    rta_frame_ctx *c = new rta_frame_ctx();
+    c->cap = max_rays;
+    const uint32_t tiles = (max_rays + kBounceTile - 1) / kBounceTile;
+    cudaError_t e = cudaSuccess;
+    e = e ? e : cudaMalloc(&c->orig, (size_t)max_rays * 12);
+    e = e ? e : cudaMalloc(&c->dir, (size_t)max_rays * 12);
+    e = e ? e : cudaMalloc(&c->maxt, (size_t)max_rays * 4);
+    e = e ? e : cudaMalloc(&c->src, (size_t)max_rays * 4);
+    e = e ? e : cudaMalloc(&c->hits, (size_t)max_rays * sizeof(HitRec));
+    e = e ? e : cudaMalloc(&c->tstat, (size_t)tiles * 4);
+    e = e ? e : cudaMalloc(&c->fs, sizeof(FrameState));
+    e = e ? e : cudaMemset(c->fs, 0, sizeof(FrameState));
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "rta_frame_create");
+        rta_frame_destroy(c);
+        return e == cudaErrorMemoryAllocation ? RTA_ERR_NOMEM : RTA_ERR_CUDA;
+    }
+    *out = c;
+    return RTA_OK;
+}
+
+int rta_frame_destroy(rta_frame_ctx *c)
+{
+    if (!c) return RTA_ERR_INVALID;
+    void *ptrs[] = {c->orig, c->dir, c->maxt, c->src, c->hits, c->tstat, c->fs};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete c;
+    return RTA_OK;
+}
+
+int rta_frame_get(const rta_frame_ctx *c, rta_frame *out)
+{
+    if (!c || !out) return RTA_ERR_INVALID;
+    out->orig = c->orig;
+    out->dir = c->dir;
+    out->maxt = c->maxt;
+    out->src = c->src;
+    out->hits = c->hits;
+    out->count = &c->fs->count;
+    out->capacity = c->cap;
+    return RTA_OK;
+}
+
+int rta_diffuse_bounce(rta_frame_ctx *c, const rta_lbvh *bvh, const float *orig, const float *dir,
+                       const void *hits, uint32_t nrays, uint32_t seed, float eps,
+                       rta_stream_t stream)
+{
+    if (!c || !bvh || !orig || !dir || !hits || nrays == 0 || nrays > c->cap) return RTA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t tiles = (nrays + kBounceTile - 1) / kBounceTile;
+    RTA_CUDA_TRY(cudaMemsetAsync(c->tstat, 0, (size_t)tiles * 4, s));
+    RTA_CUDA_TRY(cudaMemsetAsync(&c->fs->tile_ctr, 0, 4, s));
+    k_bounce<<<tiles, kBounceThreads, 0, s>>>((const TriRec *)bvh->tris, orig, dir,
+                                              (const HitRec *)hits, nrays, seed, eps, c->orig,
+                                              c->dir, c->maxt, c->src, c->tstat, c->fs, bvh->n);
+    return check_launch("k_bounce");
+}
+
+int rta_frame_run(rta_frame_ctx *c, const rta_lbvh *bvh, const float *orig, const float *dir,
+                  const float *maxt, uint32_t nrays, void *hits, uint32_t mode, uint32_t seed,
+                  float eps, rta_stream_t stream)
+{
+    if (!c || !bvh || !orig || !dir || !maxt || !hits || nrays == 0 || nrays > c->cap)
+        return RTA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t mode_nostats = mode & ~RTA_TRACE_STATS;
+    const uint32_t rb = (nrays + 255) / 256 < 4096 ? (nrays + 255) / 256 : 4096;
+    k_reset<<<rb, 256, 0, s>>>((HitRec *)hits, nrays, nullptr);
+    int rc = check_launch("k_reset");
+    if (rc) return rc;
+    rc = trace_impl(bvh, orig, dir, maxt, nrays, nullptr, hits, mode_nostats, nullptr, &c->fs->queue, s);
+    if (rc) return rc;
+    rc = rta_diffuse_bounce(c, bvh, orig, dir, hits, nrays, seed, eps, stream);
+    if (rc) return rc;
+    k_reset<<<rb, 256, 0, s>>>(c->hits, nrays, &c->fs->count);
+    if ((rc = check_launch("k_reset"))) return rc;
+    return trace_impl(bvh, c->orig, c->dir, c->maxt, nrays, &c->fs->count, c->hits, mode_nostats,
+                      nullptr, &c->fs->queue, s);
+}
+
+int rta_frame_status(rta_frame_ctx *c, rta_stream_t stream, uint32_t *flags)
+{
+    if (!c || !flags) return RTA_ERR_INVALID;
+    RTA_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    FrameState fs;
+    RTA_CUDA_TRY(cudaMemcpy(&fs, c->fs, sizeof(fs), cudaMemcpyDeviceToHost));
+    *flags = fs.status;
+    return RTA_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,384 @@
+// trace.cu -- binary-BVH traversal on sm_103a.
+//
+// Persistent warps pull batches of 32 rays from a global atomic queue; each
+// lane traverses one ray with a short stack in local memory (L1-resident).
+// The arithmetic is the reference's, operation for operation, through
+// explicit round-to-nearest intrinsics so no multiply-add is ever fused:
+//   slab test        intersect_aabb          (librta/intersect.h:56-150)
+//   Aila box test    intersect_aabb_aila     (librta/intersect.h:165-176)
+//   triangle test    intersect_tri_opt       (librta/intersect.h:8-53)
+// and the visiting order is that of the 2F4 kernels
+//   CIS  trace_cis(float4*)  (bbvh-cuda/kernels.cu:777-855)
+//   DIS  trace_dis(float4*)  (bbvh-cuda/kernels.cu:486-548)
+// so hits, including which of two equal-t triangles wins, are the reference's.
+#include "common.cuh"
+
+namespace rta {
+
+struct TraceArgs {
+    const NodeRec *nodes;
+    const RootRec *root;
+    const TriRec *tris;
+    const float *orig, *dir, *maxt;
+    uint32_t nrays;
+    const uint32_t *d_nrays;
+    HitRec *hits;
+    uint32_t *stats;
+    uint32_t *queue;    // ray batch counter, zero at launch
+    uint32_t *status;
+    uint32_t n_tris;    // bounds every link and triangle index before use
+};
+
+// intersect_aabb: per-axis division, zero-direction special case, early outs
+__device__ __forceinline__ bool slab_test(float lx, float hx, float ly, float hy, float lz, float hz,
+                                          const float o[3], const float d[3], float &dist)
+{
+    float t_near = -FLT_MAX, t_far = FLT_MAX;
+    const float lo[3] = {lx, ly, lz}, hi[3] = {hx, hy, hz};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (d[k] == 0.0f) {
+            if (o[k] < lo[k] || o[k] > hi[k]) return false;
+        } else {
+            float t1 = __fdiv_rn(__fsub_rn(lo[k], o[k]), d[k]);
+            float t2 = __fdiv_rn(__fsub_rn(hi[k], o[k]), d[k]);
+            if (t1 > t2) { float tmp = t1; t1 = t2; t2 = tmp; }
+            if (t1 > t_near) t_near = t1;
+            if (t2 < t_far) t_far = t2;
+            if (t_near > t_far) return false;
+            if (t_far < 0.0f) return false;
+        }
+    }
+    dist = t_near;
+    return true;
+}
+
+// intersect_aabb_aila with the ailabox kernels' reciprocal (kernels.cu:966-970)
+__device__ __forceinline__ bool aila_test(float lx, float hx, float ly, float hy, float lz, float hz,
+                                          const float o[3], const float id[3], float t, float &ret)
+{
+    const float lo[3] = {lx, ly, lz}, hi[3] = {hx, hy, hz};
+    float t1[3], t2[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float oid = __fmul_rn(o[k], id[k]);
+        t1[k] = __fsub_rn(__fmul_rn(lo[k], id[k]), oid);
+        t2[k] = __fsub_rn(__fmul_rn(hi[k], id[k]), oid);
+    }
+    float near = fmaxf(fmaxf(fminf(t1[0], t2[0]), fminf(t1[1], t2[1])), fminf(t1[2], t2[2]));
+    float far = fminf(fminf(fmaxf(t1[0], t2[0]), fmaxf(t1[1], t2[1])), fmaxf(t1[2], t2[2]));
+    ret = near;
+    return near <= far && far >= 0.f && near < t;
+}
+
+// intersect_tri_opt, expression for expression
+__device__ __forceinline__ bool tri_test(const TriRec &T, const float o[3], const float dir[3],
+                                         float &tt_out, float &beta_out, float &gamma_out)
+{
+    const float a_x = T.v0.x, a_y = T.v0.y, a_z = T.v0.z;
+    const float a = __fsub_rn(a_x, T.v1.x);
+    const float b = __fsub_rn(a_y, T.v1.y);
+    const float c = __fsub_rn(a_z, T.v1.z);
+    const float d = __fsub_rn(a_x, T.v2.x);
+    const float e = __fsub_rn(a_y, T.v2.y);
+    const float f = __fsub_rn(a_z, T.v2.z);
+    const float g = dir[0], h = dir[1], i = dir[2];
+    const float j = __fsub_rn(a_x, o[0]);
+    const float k = __fsub_rn(a_y, o[1]);
+    const float l = __fsub_rn(a_z, o[2]);
+    float common1 = __fsub_rn(__fmul_rn(e, i), __fmul_rn(h, f));
+    float common2 = __fsub_rn(__fmul_rn(g, f), __fmul_rn(d, i));
+    float common3 = __fsub_rn(__fmul_rn(d, h), __fmul_rn(e, g));
+    float M = __fadd_rn(__fadd_rn(__fmul_rn(a, common1), __fmul_rn(b, common2)), __fmul_rn(c, common3));
+    float beta = __fadd_rn(__fadd_rn(__fmul_rn(j, common1), __fmul_rn(k, common2)), __fmul_rn(l, common3));
+    common1 = __fsub_rn(__fmul_rn(a, k), __fmul_rn(j, b));
+    common2 = __fsub_rn(__fmul_rn(j, c), __fmul_rn(a, l));
+    common3 = __fsub_rn(__fmul_rn(b, l), __fmul_rn(k, c));
+    float gamma = __fadd_rn(__fadd_rn(__fmul_rn(i, common1), __fmul_rn(h, common2)), __fmul_rn(g, common3));
+    float tt = -__fadd_rn(__fadd_rn(__fmul_rn(f, common1), __fmul_rn(e, common2)), __fmul_rn(d, common3));
+    beta = __fdiv_rn(beta, M);
+    gamma = __fdiv_rn(gamma, M);
+    tt = __fdiv_rn(tt, M);
+    if (tt > 0.0f && beta > 0.0f && gamma > 0.0f && __fadd_rn(beta, gamma) <= 1.0f) {
+        tt_out = tt;
+        beta_out = beta;
+        gamma_out = gamma;
+        return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ NodeRec load_node(const NodeRec *nodes, uint32_t idx)
+{
+    const float4 *p = reinterpret_cast<const float4 *>(nodes + idx);
+    NodeRec r;
+    r.q0 = __ldg(p + 0);
+    r.q1 = __ldg(p + 1);
+    r.q2 = __ldg(p + 2);
+    float4 q3 = __ldg(p + 3);
+    r.q3 = make_uint4(__float_as_uint(q3.x), __float_as_uint(q3.y), __float_as_uint(q3.z),
+                      __float_as_uint(q3.w));
+    return r;
+}
+
+__device__ __forceinline__ TriRec load_tri(const TriRec *tris, uint32_t idx)
+{
+    const float4 *p = reinterpret_cast<const float4 *>(tris + idx);
+    TriRec t;
+    t.v0 = __ldg(p + 0);
+    t.v1 = __ldg(p + 1);
+    t.v2 = __ldg(p + 2);
+    return t;
+}
+
+// no ray visits more nodes than this; a corrupt tree ends the ray with a flag
+constexpr uint32_t kMaxSteps = 1u << 22;
+
+struct Best {
+    float t, beta, gamma;
+    uint32_t ref;
+};
+
+// tests the triangles of one leaf; returns true if a shadow ray may stop
+template <bool SHADOW>
+__device__ __forceinline__ bool visit_leaf(const TriRec *tris, uint32_t n_tris, uint32_t link,
+                                           const float o[3], const float d[3], float tmax, Best &best,
+                                           uint32_t &tri_tests, bool &bad)
+{
+    const uint32_t first = leaf_first(link);
+    if (first >= n_tris) { bad = true; return true; }
+    TriRec t0 = load_tri(tris, first);
+    uint32_t f = leaf_count_field(link);
+    uint32_t count = f < 63u ? f + 1u : __float_as_uint(t0.v0.w);
+    if (count > n_tris - first) { bad = true; return true; }
+    for (uint32_t i = 0; i < count; ++i) {
+        TriRec T = i ? load_tri(tris, first + i) : t0;
+        ++tri_tests;
+        float t, b, g;
+        if (tri_test(T, o, d, t, b, g)) {
+            if (t < best.t && t <= tmax) {
+                best.t = t;
+                best.beta = b;
+                best.gamma = g;
+                best.ref = first + i;
+                if (SHADOW) break;
+            }
+        }
+    }
+    return SHADOW && best.t != FLT_MAX;
+}
+
+template <bool DIS, bool SHADOW, bool AILA, bool STATS, int STACK>
+__global__ void __launch_bounds__(128) k_trace(TraceArgs A)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nrays = A.d_nrays ? *A.d_nrays : A.nrays;
+    const RootRec root = *A.root;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(A.queue, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= nrays) break;
+        const uint32_t r = base + lane;
+        if (r >= nrays) continue;
+
+        float o[3], d[3];
+        o[0] = A.orig[3 * (size_t)r + 0];
+        o[1] = A.orig[3 * (size_t)r + 1];
+        o[2] = A.orig[3 * (size_t)r + 2];
+        d[0] = A.dir[3 * (size_t)r + 0];
+        d[1] = A.dir[3 * (size_t)r + 1];
+        d[2] = A.dir[3 * (size_t)r + 2];
+        const float tmax = A.maxt[r];
+        float id[3] = {0.f, 0.f, 0.f};
+        if (AILA) {
+            const float ooeps = 8.27180612553027674871e-25f;   // exp2f(-80)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                id[k] = __fdiv_rn(1.0f, fabsf(d[k]) > ooeps ? d[k] : copysignf(ooeps, d[k]));
+        }
+        Best best;
+        best.t = FLT_MAX;
+        best.beta = best.gamma = 0.f;
+        best.ref = 0;
+        uint32_t stack[STACK];
+        int sp = -1;
+        uint32_t inner_visits = 0, tri_tests = 0;
+        bool overflow = false, capped = false, bad = false;
+        const uint32_t n_inner = A.n_tris - 1u;
+
+        if (!DIS) {
+            // child-is: the current node's children are tested together
+            uint32_t cur = root.link;
+            for (uint32_t steps = 0;; ++steps) {
+                if (steps >= kMaxSteps) { capped = true; break; }
+                if (!is_leaf(cur)) {
+                    if (cur >= n_inner) { bad = true; break; }
+                    ++inner_visits;
+                    const NodeRec nd = load_node(A.nodes, cur);
+                    float dl = FLT_MAX, dr = FLT_MAX;
+                    bool hl, hr;
+                    if (AILA) {
+                        hl = aila_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, o, id, best.t, dl);
+                        hr = aila_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, o, id, best.t, dr);
+                    } else {
+                        hl = slab_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, o, d, dl);
+                        hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, o, d, dr);
+                    }
+                    if (dl >= best.t || dl > tmax) hl = false;
+                    if (dr >= best.t || dr > tmax) hr = false;
+                    if (hl && hr) {
+                        if (sp + 1 >= STACK) { overflow = true; break; }
+                        if (dl <= dr) { stack[++sp] = nd.q3.y; cur = nd.q3.x; }
+                        else { stack[++sp] = nd.q3.x; cur = nd.q3.y; }
+                    } else if (hl) {
+                        cur = nd.q3.x;
+                    } else if (hr) {
+                        cur = nd.q3.y;
+                    } else {
+                        if (sp < 0) break;
+                        cur = stack[sp--];
+                    }
+                } else {
+                    if (visit_leaf<SHADOW>(A.tris, A.n_tris, cur, o, d, tmax, best, tri_tests, bad)) break;
+                    if (sp < 0) break;
+                    cur = stack[sp--];
+                }
+            }
+        } else {
+            // direct-is: a node's own box is tested when it is visited; the
+            // stack holds (parent << 1 | side) so a popped node's box is re-read
+            // from its parent's record
+            uint32_t cur = root.link;
+            float bx[6] = {root.lo[0], root.hi[0], root.lo[1], root.hi[1], root.lo[2], root.hi[2]};
+            float dist = FLT_MAX;
+            for (uint32_t steps = 0;; ++steps) {
+                if (steps >= kMaxSteps) { capped = true; break; }
+                bool pop = false;
+                if (!is_leaf(cur)) {
+                    ++inner_visits;
+                    bool h = AILA ? aila_test(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], o, id, best.t, dist)
+                                  : slab_test(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], o, d, dist);
+                    if (dist >= best.t || dist > tmax) h = false;
+                    if (h) {
+                        if (sp + 1 >= STACK) { overflow = true; break; }
+                        if (cur >= n_inner) { bad = true; break; }
+                        const NodeRec nd = load_node(A.nodes, cur);
+                        stack[++sp] = (cur << 1) | 1u;
+                        cur = nd.q3.x;
+                        bx[0] = nd.q0.x; bx[1] = nd.q0.y; bx[2] = nd.q0.z;
+                        bx[3] = nd.q0.w; bx[4] = nd.q1.x; bx[5] = nd.q1.y;
+                    } else {
+                        pop = true;
+                    }
+                } else {
+                    if (visit_leaf<SHADOW>(A.tris, A.n_tris, cur, o, d, tmax, best, tri_tests, bad)) break;
+                    pop = true;
+                }
+                if (pop) {
+                    if (sp < 0) break;
+                    const uint32_t e = stack[sp--];
+                    if ((e >> 1) >= n_inner) { bad = true; break; }
+                    const NodeRec nd = load_node(A.nodes, e >> 1);
+                    if (e & 1u) {
+                        cur = nd.q3.y;
+                        bx[0] = nd.q1.z; bx[1] = nd.q1.w; bx[2] = nd.q2.x;
+                        bx[3] = nd.q2.y; bx[4] = nd.q2.z; bx[5] = nd.q2.w;
+                    } else {
+                        cur = nd.q3.x;
+                        bx[0] = nd.q0.x; bx[1] = nd.q0.y; bx[2] = nd.q0.z;
+                        bx[3] = nd.q0.w; bx[4] = nd.q1.x; bx[5] = nd.q1.y;
+                    }
+                }
+            }
+        }
+        if (overflow) atomicOr(A.status, RTA_DEV_STACK_OVERFLOW);
+        if (capped) atomicOr(A.status, RTA_DEV_ITER_LIMIT);
+        if (bad) atomicOr(A.status, RTA_DEV_BAD_LINK);
+        if (best.t != FLT_MAX) {
+            reinterpret_cast<float4 *>(A.hits)[r] =
+                make_float4(best.t, best.beta, best.gamma, __uint_as_float(best.ref));
+        } else {
+            A.hits[r].t = FLT_MAX;
+        }
+        if (STATS) {
+            A.stats[2 * (size_t)r + 0] = inner_visits;
+            A.stats[2 * (size_t)r + 1] = tri_tests;
+        }
+    }
+}
+
+template <bool DIS, bool SHADOW, bool AILA, bool STATS, int STACK>
+static int launch_trace(const TraceArgs &a, cudaStream_t s)
+{
+    static int blocks = 0;
+    if (!blocks) {
+        int per_sm = 0, dev = 0, sms = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<DIS, SHADOW, AILA, STATS, STACK>, 128, 0);
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    }
+    k_trace<DIS, SHADOW, AILA, STATS, STACK><<<blocks, 128, 0, s>>>(a);
+    return check_launch("k_trace");
+}
+
+template <int STACK>
+static int dispatch(const TraceArgs &a, uint32_t mode, cudaStream_t s)
+{
+    const bool dis = mode & RTA_TRACE_DIS, sh = mode & RTA_TRACE_SHADOW, ai = mode & RTA_TRACE_AILA,
+               st = mode & RTA_TRACE_STATS;
+#define RTA_CASE(D, S, A, T) \
+    if (dis == D && sh == S && ai == A && st == T) return launch_trace<D, S, A, T, STACK>(a, s);
+    RTA_CASE(false, false, false, false) RTA_CASE(false, false, false, true)
+    RTA_CASE(false, true, false, false) RTA_CASE(false, true, false, true)
+    RTA_CASE(false, false, true, false) RTA_CASE(false, false, true, true)
+    RTA_CASE(false, true, true, false) RTA_CASE(false, true, true, true)
+    RTA_CASE(true, false, false, false) RTA_CASE(true, false, false, true)
+    RTA_CASE(true, true, false, false) RTA_CASE(true, true, false, true)
+    RTA_CASE(true, false, true, false) RTA_CASE(true, false, true, true)
+    RTA_CASE(true, true, true, false) RTA_CASE(true, true, true, true)
+#undef RTA_CASE
+    return RTA_ERR_INVALID;
+}
+
+// the tree depth after the equal-code collapse is at most the number of code
+// bits + 1, which bounds the stack (one push per level)
+int trace_impl(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt,
+               uint32_t nrays, const uint32_t *d_nrays, void *hits, uint32_t mode, uint32_t *stats,
+               uint32_t *queue, cudaStream_t s)
+{
+    TraceArgs a;
+    a.nodes = (const NodeRec *)bvh->nodes;
+    a.root = (const RootRec *)bvh->root;
+    a.tris = (const TriRec *)bvh->tris;
+    a.orig = orig;
+    a.dir = dir;
+    a.maxt = maxt;
+    a.nrays = nrays;
+    a.d_nrays = d_nrays;
+    a.hits = (HitRec *)hits;
+    a.stats = stats;
+    a.queue = queue;
+    a.status = bvh->status;
+    a.n_tris = bvh->n;
+    RTA_CUDA_TRY(cudaMemsetAsync(queue, 0, 4, s));
+    if (bvh->morton_bits == 63) return dispatch<80>(a, mode, s);
+    return dispatch<40>(a, mode, s);
+}
+
+} // namespace rta
+
+using namespace rta;
+
+extern "C" int rta_trace(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt,
+                         uint32_t nrays, const uint32_t *d_nrays, void *hits, uint32_t mode,
+                         uint32_t *stats, rta_stream_t stream)
+{
+    if (!bvh || !orig || !dir || !maxt || !hits || (!d_nrays && nrays == 0)) return RTA_ERR_INVALID;
+    if ((mode & RTA_TRACE_STATS) && !stats) return RTA_ERR_INVALID;
+    // the queue word lives after the status word in the context's status block
+    uint32_t *queue = bvh->status + 4;
+    return trace_impl(bvh, orig, dir, maxt, nrays, d_nrays, hits, mode, stats, queue,
+                      (cudaStream_t)stream);
+}

@@ -1,0 +1,100 @@
+"""ctypes binding of the C ABI in include/rta_gb300.h.
+
+Device memory is handed over as raw pointers (for example ``tensor.data_ptr()``
+of a CUDA torch tensor) and streams as raw ``cudaStream_t`` handles
+(``torch.cuda.current_stream().cuda_stream``).  Loading fails loudly when the
+library has not been built: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "librta_gb300.so")
+
+OK = 0
+ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_NOMEM = -1, -2, -3, -4
+DEV_STACK_OVERFLOW, DEV_SPIN_TIMEOUT, DEV_QUANT_WRAP, DEV_ZERO_EXTENT, DEV_ITER_LIMIT, DEV_BAD_LINK = 1, 2, 4, 8, 16, 32
+TRACE_CIS, TRACE_DIS, TRACE_SHADOW, TRACE_AILA, TRACE_STATS = 0, 1, 2, 4, 8
+
+# every symbol include/rta_gb300.h declares
+SYMBOLS = [
+    "rta_last_error", "rta_lbvh_max_triangles", "rta_lbvh_create", "rta_lbvh_destroy",
+    "rta_lbvh_reserve", "rta_lbvh_build", "rta_lbvh_get", "rta_lbvh_status", "rta_lbvh_to_2f4",
+    "rta_trace", "rta_setup_shirley_rays", "rta_reset_intersections", "rta_frame_create",
+    "rta_frame_destroy", "rta_frame_get", "rta_diffuse_bounce", "rta_frame_run",
+    "rta_frame_status",
+]
+
+
+class RtaError(RuntimeError):
+    pass
+
+
+class LbvhView(C.Structure):
+    """struct rta_lbvh"""
+    _fields_ = [("nodes", C.c_void_p), ("root", C.c_void_p), ("tris", C.c_void_p),
+                ("index", C.c_void_p), ("codes", C.c_void_p), ("parents", C.c_void_p),
+                ("n", C.c_uint32), ("morton_bits", C.c_int32), ("status", C.c_void_p)]
+
+
+class FrameView(C.Structure):
+    """struct rta_frame"""
+    _fields_ = [("orig", C.c_void_p), ("dir", C.c_void_p), ("maxt", C.c_void_p),
+                ("src", C.c_void_p), ("hits", C.c_void_p), ("count", C.c_void_p),
+                ("capacity", C.c_uint32)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RtaError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; "
+                       f"g.build()'` (there is no CPU fallback)")
+    L = C.CDLL(path)
+    vp, u32, i32, f32 = C.c_void_p, C.c_uint32, C.c_int32, C.c_float
+    P = C.POINTER
+    L.rta_last_error.restype = C.c_char_p
+    L.rta_lbvh_max_triangles.restype = u32
+    L.rta_lbvh_create.argtypes = [P(vp)]
+    L.rta_lbvh_destroy.argtypes = [vp]
+    L.rta_lbvh_reserve.argtypes = [vp, u32, i32]
+    L.rta_lbvh_build.argtypes = [vp, vp, u32, i32, vp, vp]
+    L.rta_lbvh_get.argtypes = [vp, P(LbvhView)]
+    L.rta_lbvh_status.argtypes = [P(LbvhView), vp, P(u32)]
+    L.rta_lbvh_to_2f4.argtypes = [P(LbvhView), vp, vp]
+    L.rta_trace.argtypes = [P(LbvhView), vp, vp, vp, u32, vp, vp, u32, vp, vp]
+    L.rta_setup_shirley_rays.argtypes = [vp, vp, vp, f32, f32, i32, i32, vp, vp, vp, f32, vp]
+    L.rta_reset_intersections.argtypes = [vp, u32, u32, vp]
+    L.rta_frame_create.argtypes = [P(vp), u32]
+    L.rta_frame_destroy.argtypes = [vp]
+    L.rta_frame_get.argtypes = [vp, P(FrameView)]
+    L.rta_diffuse_bounce.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, u32, f32, vp]
+    L.rta_frame_run.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, vp, u32, u32, f32, vp]
+    L.rta_frame_status.argtypes = [vp, vp, P(u32)]
+    for name in SYMBOLS:
+        fn = getattr(L, name)
+        if fn.restype is None or fn.restype is C.c_int:
+            if name not in ("rta_last_error", "rta_lbvh_max_triangles"):
+                fn.restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(rc: int, what: str) -> None:
+    if rc != OK:
+        msg = load().rta_last_error().decode(errors="replace")
+        raise RtaError(f"{what} failed with status {rc}: {msg}")
+
+
+def stream_handle(stream) -> C.c_void_p:
+    """Accepts None, an int handle or a torch.cuda.Stream."""
+    if stream is None:
+        return C.c_void_p(0)
+    h = getattr(stream, "cuda_stream", stream)
+    return C.c_void_p(int(h))

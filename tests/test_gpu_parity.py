@@ -1,0 +1,292 @@
+"""GPU parity: the sm_103a build and traversal, called through the C ABI,
+against the golden fixtures made by the reference's own code and against the
+CPU oracle.  Everything is compared bit for bit: Morton codes, sorted ids,
+every word of the 2F4 node array, the camera rays, and t / beta / gamma / ref
+of every hit."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from oracle import oracle as O  # noqa: E402
+from rta_gb300 import lib as L  # noqa: E402
+from rta_gb300 import plugin as P  # noqa: E402
+from rta_gb300 import scenes as S  # noqa: E402
+
+MODES = {"cis": L.TRACE_CIS, "dis": L.TRACE_DIS, "shadow_cis": L.TRACE_CIS | L.TRACE_SHADOW,
+         "shadow_dis": L.TRACE_DIS | L.TRACE_SHADOW, "cis_aila": L.TRACE_CIS | L.TRACE_AILA,
+         "dis_aila": L.TRACE_DIS | L.TRACE_AILA}
+ORC = {"cis": O.CIS, "dis": O.DIS, "shadow_cis": O.CIS | O.SHADOW, "shadow_dis": O.DIS | O.SHADOW,
+       "cis_aila": O.CIS | O.AILA, "dis_aila": O.DIS | O.AILA}
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def records(pos):
+    p = np.asarray(pos, np.float32).reshape(-1, 3, 3)
+    return S._records(p[:, 0], p[:, 1], p[:, 2])
+
+
+def gpu_build(tris, bits=30):
+    ctor = P.lbvh_constructor(morton_bits=bits)
+    bvh = ctor.build(P.cuda_ftl(tris))
+    bvh._ctor_ref = ctor   # keep the buffers alive with the view
+    return bvh
+
+
+def gpu_trace(bvh, orig, dirs, maxt, mode, hits_init=None, stats=False):
+    dev = torch.device("cuda")
+    o = torch.from_numpy(np.ascontiguousarray(orig, np.float32).reshape(-1)).to(dev)
+    d = torch.from_numpy(np.ascontiguousarray(dirs, np.float32).reshape(-1)).to(dev)
+    m = torch.from_numpy(np.ascontiguousarray(maxt, np.float32).reshape(-1)).to(dev)
+    n = m.shape[0]
+    if hits_init is None:
+        hits_init = O.reset_hits(n)
+    h = torch.from_numpy(np.ascontiguousarray(hits_init).view(np.float32).reshape(-1).copy()).to(dev)
+    st = torch.zeros(2 * n, dtype=torch.int32, device=dev) if stats else None
+    import ctypes as C
+    L.check(L.load().rta_trace(C.byref(bvh.view), P._ptr(o), P._ptr(d), P._ptr(m), n, C.c_void_p(0),
+                               P._ptr(h), mode | (L.TRACE_STATS if stats else 0), P._ptr(st),
+                               P._stream()), "rta_trace")
+    torch.cuda.synchronize()
+    out = h.cpu().numpy().view(O.HIT_DTYPE)
+    if stats:
+        return out, st.cpu().numpy().view(np.uint32).reshape(-1, 2)
+    return out
+
+
+def assert_hits_equal(a, b):
+    for f in ("t", "beta", "gamma"):
+        np.testing.assert_array_equal(a[f].view(np.uint32), b[f].view(np.uint32), err_msg=f)
+    valid = a["t"] != np.float32(S.FLT_MAX)
+    np.testing.assert_array_equal(a["ref"][valid], b["ref"][valid], err_msg="ref")
+
+
+def assert_build_equals(bvh, codes, ids, nodes):
+    np.testing.assert_array_equal(bvh.codes(), codes)
+    np.testing.assert_array_equal(bvh.index_buffer, ids)
+    np.testing.assert_array_equal(bvh.node_data_2f4().view(np.uint32), np.asarray(nodes).view(np.uint32))
+    assert bvh.status() & ~(L.DEV_QUANT_WRAP | L.DEV_ZERO_EXTENT) == 0
+
+
+# --------------------------------------------------------------------------- #
+# LBVH                                                                         #
+# --------------------------------------------------------------------------- #
+
+@pytest.mark.parametrize("case", ["n1", "n2", "n3", "n7", "dup64", "rand100", "clump",
+                                  "terrain16x8", "clusters4x64", "sphere"])
+def test_build_matches_reference_golden(golden_dir, case):
+    z = np.load(os.path.join(golden_dir, "lbvh_cases.npz"))
+    bvh = gpu_build(records(z[f"{case}/pos"]), 30)
+    assert_build_equals(bvh, z[f"{case}/codes"], z[f"{case}/ids"], z[f"{case}/nodes"])
+
+
+@pytest.mark.parametrize("scene,bits", [("terrain", 30), ("clusters", 30), ("clusters", 63),
+                                        ("terrain", 63)])
+def test_build_matches_oracle(scene, bits):
+    tris = S.terrain(256, 128, seed=2) if scene == "terrain" else S.clusters(32, 2048, seed=3)
+    lb = O.lbvh_build(tris, bits)
+    bvh = gpu_build(tris, bits)
+    codes = lb.codes if bits == 63 else lb.codes.astype(np.uint32)
+    assert_build_equals(bvh, codes, lb.ids, lb.nodes)
+    # the Morton-ordered 104-byte records the AS exposes (lbvh-kernels.cu:557-578)
+    np.testing.assert_array_equal(bvh.canonical_triangle_ptr().view(np.uint32),
+                                  O.permute(tris, lb.ids).view(np.uint32))
+
+
+def test_rebuild_reuses_buffers_and_matches():
+    """Rebuilding with a second, smaller scene through the same constructor
+    (the -R path, rta/main.cpp:389-400) gives that scene's tree."""
+    ctor = P.lbvh_constructor(morton_bits=30)
+    big = S.terrain(128, 64, seed=4)
+    small = S.clusters(4, 1000, seed=6)
+    ctor.build(P.cuda_ftl(big))
+    bvh = ctor.build(P.cuda_ftl(small))
+    lb = O.lbvh_build(small, 30)
+    assert_build_equals(bvh, lb.codes.astype(np.uint32), lb.ids, lb.nodes)
+
+
+# --------------------------------------------------------------------------- #
+# rays and traversal                                                           #
+# --------------------------------------------------------------------------- #
+
+def test_camera_kernel_matches_reference_golden(golden_dir):
+    z = np.load(os.path.join(golden_dir, "sphere_trace.npz"))
+    g = P.cam_ray_generator_shirley(int(z["w"]), int(z["h"]))
+    g.setup(z["cam_pos"], z["cam_dir"], z["cam_up"], 60.0)
+    import ctypes as C
+    L.check(L.load().rta_setup_shirley_rays(
+        P._ptr(g.gpu_direction), P._ptr(g.gpu_origin), P._ptr(g.gpu_maxt), float(z["tan_half"]),
+        float(g.aspect), g.w, g.h, (C.c_float * 3)(*z["cam_dir"].tolist()),
+        (C.c_float * 3)(*z["cam_pos"].tolist()), (C.c_float * 3)(*z["cam_up"].tolist()),
+        S.FLT_MAX, P._stream()), "rta_setup_shirley_rays")
+    torch.cuda.synchronize()
+    rays = np.concatenate([g.gpu_origin.cpu().numpy().reshape(-1, 3),
+                           g.gpu_direction.cpu().numpy().reshape(-1, 3),
+                           g.gpu_maxt.cpu().numpy()[:, None]], axis=1)
+    assert sha(rays.astype(np.float32)) == str(z["rays_sha"])
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_trace_matches_reference_golden(golden_dir, mode):
+    z = np.load(os.path.join(golden_dir, "sphere_trace.npz"))
+    tris = records(z["pos"])
+    bvh = gpu_build(tris)
+    o, d, m = O.shirley_rays(z["tan_half"], np.float32(np.float32(z["w"]) / np.float32(z["h"])),
+                             int(z["w"]), int(z["h"]), z["cam_dir"], z["cam_pos"], z["cam_up"])
+    hits = gpu_trace(bvh, o, d, m, MODES[mode])
+    if mode == "cis":
+        assert_hits_equal(hits, z["cis_hits"])
+    assert sha(hits) == str(z[f"{mode}_sha"])
+
+
+def test_trace_matches_cpu_plugin_golden(golden_dir):
+    """Config 1: hits by original triangle id equal the reference CPU plugin's."""
+    z = np.load(os.path.join(golden_dir, "sphere_trace.npz"))
+    bvh = gpu_build(records(z["pos"]))
+    o, d, m = O.shirley_rays(z["tan_half"], np.float32(np.float32(z["w"]) / np.float32(z["h"])),
+                             int(z["w"]), int(z["h"]), z["cam_dir"], z["cam_pos"], z["cam_up"])
+    hits = gpu_trace(bvh, o, d, m, L.TRACE_CIS)
+    valid = hits["t"] != np.float32(S.FLT_MAX)
+    ids = np.where(valid, bvh.index_buffer[hits["ref"]], np.uint32(0xFFFFFFFF))
+    np.testing.assert_array_equal(ids, z["bbvh_id"])
+    np.testing.assert_array_equal(hits["t"].view(np.uint32), z["bbvh_t"].view(np.uint32))
+
+
+@pytest.mark.parametrize("mode", ["cis", "dis"])
+def test_terrain_trace_matches_reference_golden(golden_dir, mode):
+    z = np.load(os.path.join(golden_dir, "terrain_trace.npz"))
+    bvh = gpu_build(records(z["pos"]))
+    o, d, m = O.shirley_rays(z["tan_half"], np.float32(np.float32(z["w"]) / np.float32(z["h"])),
+                             int(z["w"]), int(z["h"]), z["cam_dir"], z["cam_pos"], z["cam_up"])
+    hits = gpu_trace(bvh, o, d, m, MODES[mode])
+    assert sha(hits) == sha(z[f"{mode}_hits"])
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_trace_matches_oracle_terrain(mode):
+    tris = S.terrain(256, 128, seed=7)
+    lb = O.lbvh_build(tris, 30)
+    srt = O.permute(tris, lb.ids)
+    cam = S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), fovy=60.0, w=480, h=270)
+    o, d, m = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
+    ref, _, _ = O.trace(lb.nodes, srt, o, d, m, ORC[mode], 64)
+    bvh = gpu_build(tris)
+    assert_hits_equal(gpu_trace(bvh, o, d, m, MODES[mode]), ref)
+
+
+@pytest.mark.parametrize("bits", [30, 63])
+@pytest.mark.parametrize("mode", ["cis", "dis", "shadow_cis"])
+def test_trace_matches_oracle_incoherent(bits, mode):
+    tris = S.clusters(64, 1024, seed=9)
+    lb = O.lbvh_build(tris, bits)
+    srt = O.permute(tris, lb.ids)
+    o, d, m = S.incoherent_rays(200_000, seed=9)
+    ref, st_ref, _ = O.trace(lb.nodes, srt, o, d, m, ORC[mode], 256, stats=True)
+    bvh = gpu_build(tris, bits)
+    hits, st = gpu_trace(bvh, o, d, m, MODES[mode], stats=True)
+    assert_hits_equal(hits, ref)
+    np.testing.assert_array_equal(st, st_ref)   # same visiting order, node for node
+    assert bvh.status() & L.DEV_STACK_OVERFLOW == 0
+
+
+def test_miss_keeps_record_fields():
+    """A miss writes only t (kernels.cu:794-796 reads the record first)."""
+    tris = S.terrain(8, 8)
+    bvh = gpu_build(tris)
+    o = np.array([0, 5, 0], np.float32)
+    d = np.array([0, 1, 0], np.float32)
+    init = np.zeros(1, O.HIT_DTYPE)
+    init["t"], init["beta"], init["gamma"], init["ref"] = 3.0, 0.25, 0.5, 77
+    h = gpu_trace(bvh, o, d, np.array([S.FLT_MAX], np.float32), L.TRACE_CIS, hits_init=init)
+    assert h["t"][0] == np.float32(S.FLT_MAX)
+    assert (h["beta"][0], h["gamma"][0], h["ref"][0]) == (np.float32(0.25), np.float32(0.5), 77)
+
+
+def test_max_t_is_honoured():
+    tris = S.terrain(64, 32, seed=1)
+    lb = O.lbvh_build(tris, 30)
+    srt = O.permute(tris, lb.ids)
+    cam = S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), w=160, h=90)
+    o, d, _ = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
+    m = np.full(cam.w * cam.h, 1.7, np.float32)
+    ref, _, _ = O.trace(lb.nodes, srt, o, d, m, O.CIS, 64)
+    got = gpu_trace(gpu_build(tris), o, d, m, L.TRACE_CIS)
+    assert_hits_equal(got, ref)
+    assert (got["t"][got["t"] < 3e38] <= 1.7).all()
+
+
+# --------------------------------------------------------------------------- #
+# frame: primary + one diffuse bounce                                          #
+# --------------------------------------------------------------------------- #
+
+def test_frame_bounce_matches_oracle():
+    tris = S.terrain(128, 64, seed=5)
+    cam = S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), w=320, h=180)
+    s = P.create_rt_set(tris, cam.w, cam.h)
+    s.rgen.setup(cam.pos, cam.dir, cam.up, cam.fovy)
+    b = P.diffuse_bounce_collector(cam.w, cam.h, seed=13, eps=1e-4)
+    s.rt.ray_generator(s.rgen)
+    s.rt.ray_bouncer(b)
+    s.rt.trace()
+    assert len(s.rt.timings) == 2
+    torch.cuda.synchronize()
+    prim = b.intersections()
+    o, d, m = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
+    lb = O.lbvh_build(tris, 30)
+    srt = O.permute(tris, lb.ids)
+    ref, _, _ = O.trace(lb.nodes, srt, o, d, m, O.CIS, 64)
+    assert_hits_equal(prim, ref)
+    bo, bd, bm, bsrc = O.diffuse_bounce(srt, o, d, ref, seed=13, eps=1e-4)
+    cnt = b.bounce_count()
+    assert cnt == bm.shape[0] and cnt > 0
+    f = b.frame
+    got_o = P.device_view(f.orig, 3 * cnt).cpu().numpy()
+    got_d = P.device_view(f.dir, 3 * cnt).cpu().numpy()
+    got_src = P.device_view(f.src, cnt, "<u4").cpu().numpy().view(np.uint32)
+    np.testing.assert_array_equal(got_src, bsrc)
+    np.testing.assert_array_equal(got_o.view(np.uint32), bo.view(np.uint32))
+    np.testing.assert_array_equal(got_d.view(np.uint32), bd.view(np.uint32))
+    bref, _, _ = O.trace(lb.nodes, srt, bo, bd, bm, O.CIS, 64)
+    got_h = P.device_view(f.hits, 4 * cnt).cpu().numpy().view(O.HIT_DTYPE)
+    assert_hits_equal(got_h, bref)
+
+
+def test_rebinding_contract():
+    """rt.acceleration_structure(new_as) makes the tracer use the new tree
+    (bbvh-cuda.h:89-92, rta/main.cpp:389-400)."""
+    a = S.terrain(32, 16, seed=1)
+    b = S.clusters(4, 256, seed=2)
+    s = P.create_rt_set(a, 64, 64)
+    new_as = s.ctor.build(P.cuda_ftl(b))
+    s.rt.acceleration_structure(new_as)
+    assert s.rt.acceleration_structure() is new_as and s.rt.bbvh is new_as
+
+
+# --------------------------------------------------------------------------- #
+# full configuration-2 size                                                    #
+# --------------------------------------------------------------------------- #
+
+def test_full_size_terrain_build_and_frame():
+    """1,048,576-triangle terrain and the 1920x1080 frame: the whole tree is
+    bit-identical to the oracle's, and so is every primary hit."""
+    tris = S.terrain(1024, 512, seed=0)
+    lb = O.lbvh_build(tris, 30)
+    bvh = gpu_build(tris, 30)
+    codes = bvh.codes()
+    assert (np.diff(codes.astype(np.int64)) >= 0).all()
+    ids = bvh.index_buffer
+    assert np.array_equal(np.sort(ids), np.arange(tris.shape[0], dtype=np.uint32))
+    assert_build_equals(bvh, lb.codes.astype(np.uint32), lb.ids, lb.nodes)
+    cam = S.terrain_camera()
+    o, d, m = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
+    srt = O.permute(tris, lb.ids)
+    ref, _, _ = O.trace(lb.nodes, srt, o, d, m, O.CIS, 64)
+    assert_hits_equal(gpu_trace(bvh, o, d, m, L.TRACE_CIS), ref)
