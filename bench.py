@@ -57,6 +57,17 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value: float, dist=None, device=None) -> float:
+    """The slowest rank's time: every replica runs the same frame, the job ends
+    when the last one does."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -300,11 +311,7 @@ def run_gb300(args):
             trace_ms.append(e0.elapsed_time(e1))
     if pg:
         pg.barrier()
-    total_ms = sum(step_ms)
-    if pg:
-        t = torch.tensor([total_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), pg, dev)
     ms_per_step = total_ms / args.steps
     value = rays_per_step * world * args.steps / (total_ms * 1e-3) / 1e6
 

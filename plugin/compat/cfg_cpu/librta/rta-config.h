@@ -1,4 +1,4 @@
-/* configure-generated header of the reference, written for the oracle build:
+/* configure-generated header of the reference, written for builds against the reference headers:
  * RTA_HAVE_LIBCUDART=0. */
 #ifndef ORACLE_SHIM_RTA_CONFIG_H
 #define ORACLE_SHIM_RTA_CONFIG_H

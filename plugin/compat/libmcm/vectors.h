@@ -1,7 +1,7 @@
 /* Stand-in for the absent libmcm <libmcm/vectors.h> (rta's basic_types.h:7).
  * Plain float vectors and the component-wise operations the reference CPU code
  * calls, evaluated in the operation order of librta/cuda-vec.h:157-193.
- * Part of the oracle build recipe (test infrastructure only). */
+ * Used to compile code against the reference headers (plugin/, oracle recipe). */
 #ifndef ORACLE_SHIM_LIBMCM_VECTORS_H
 #define ORACLE_SHIM_LIBMCM_VECTORS_H
 #include <math.h>

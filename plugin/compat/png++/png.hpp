@@ -1,5 +1,4 @@
-/* No-op stand-in for png++ (image output is not on the traced path).
- * Oracle build recipe only. */
+/* No-op stand-in for png++ (image output is not on the traced path). */
 #ifndef ORACLE_SHIM_PNGPP_H
 #define ORACLE_SHIM_PNGPP_H
 #include <string>
