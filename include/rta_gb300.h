@@ -177,6 +177,26 @@ int rta_frame_run(rta_frame_ctx *ctx, const rta_lbvh *bvh, const float *orig, co
 /* Synchronises and returns the frame's device status flags. */
 int rta_frame_status(rta_frame_ctx *ctx, rta_stream_t stream, uint32_t *flags);
 
+/* No counterpart in the reference.  rta_diffuse_bounce for callers that may
+ * not allocate device memory: a renderer that hands all device memory to its
+ * own pool under a fixed budget, or a frame loop that must not take
+ * cudaMalloc's implicit device synchronisation between two passes.  It calls
+ * no cudaMalloc, cudaFree or other allocating routine; its scratch (the
+ * look-back words of the ordered compaction) is a 64 KiB module array that
+ * every GPU loading the library holds until the process exits.
+ *   out_orig/out_dir/out_maxt/out_src  room for nrays bounce rays
+ *   out_count  device word: the number of bounce rays written
+ * nrays above RTA_BOUNCE_NOALLOC_MAX_RAYS returns RTA_ERR_INVALID with a
+ * message in rta_last_error().  The first call on a device looks up the
+ * scratch's device address; make that first call before any stream capture.
+ * Every call shares the scratch: calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller. */
+#define RTA_BOUNCE_NOALLOC_MAX_RAYS (1u << 24)
+int rta_diffuse_bounce_noalloc(const rta_lbvh *bvh, const float *orig, const float *dir,
+                               const void *hits, uint32_t nrays, uint32_t seed, float eps,
+                               float *out_orig, float *out_dir, float *out_maxt, uint32_t *out_src,
+                               uint32_t *out_count, rta_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

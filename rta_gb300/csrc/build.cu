@@ -32,6 +32,8 @@ void set_cuda_error(cudaError_t e, const char *where)
     g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
 }
 
+void set_error_message(const char *msg) { g_last_error = msg; }
+
 int check_launch(const char *where)
 {
     cudaError_t e = cudaGetLastError();

@@ -119,6 +119,7 @@ __device__ __forceinline__ uint32_t lookback(const uint32_t *stat, uint32_t stri
 // host-side error helpers (one translation unit defines the storage)
 namespace rta {
 void set_cuda_error(cudaError_t e, const char *where);
+void set_error_message(const char *msg);
 int check_launch(const char *where);
 }
 

@@ -6,6 +6,9 @@
 //   k_bounce    one cosine-weighted diffuse bounce ray per hit (no reference
 //               counterpart), compacted in primary-ray order by a single-pass
 //               scan with decoupled look-back
+#include <cstdio>
+#include <mutex>
+
 #include "common.cuh"
 
 namespace rta {
@@ -379,3 +382,79 @@ int rta_frame_status(rta_frame_ctx *c, rta_stream_t stream, uint32_t *flags)
 }
 
 } // extern "C"
+
+// ------------------------------------------------------------------------- //
+// allocation-free bounce                                                     //
+// ------------------------------------------------------------------------- //
+//
+// Scratch of rta_diffuse_bounce_noalloc: 4 words of FrameState (tile counter,
+// count, unused queue word, status flags) followed by one look-back word per
+// 1024-ray tile, for at most RTA_BOUNCE_NOALLOC_MAX_RAYS rays: 64 KiB + 16 B.
+// It is a module variable, so every GPU that loads the library holds it
+// until the process exits, and every call shares it.
+
+namespace rta {
+
+static_assert(RTA_BOUNCE_NOALLOC_MAX_RAYS % kBounceTile == 0, "whole tiles");
+constexpr uint32_t kNoAllocWords = 4u + RTA_BOUNCE_NOALLOC_MAX_RAYS / kBounceTile;
+static __device__ __align__(256) uint32_t g_bounce_scratch[kNoAllocWords];
+
+// host side: the device address of g_bounce_scratch, looked up once per device
+constexpr int kMaxDevices = 64;
+static std::mutex g_scratch_mu;
+static uint32_t *g_scratch_addr[kMaxDevices];
+
+static int bounce_scratch(uint32_t **out)
+{
+    int dev = -1;
+    RTA_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return RTA_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        // The symbol's name is a host-side stand-in; only this call gives the
+        // address the kernels of the current device may use.
+        void *p = nullptr;
+        RTA_CUDA_TRY(cudaGetSymbolAddress(&p, g_bounce_scratch));
+        g_scratch_addr[dev] = static_cast<uint32_t *>(p);
+    }
+    *out = g_scratch_addr[dev];
+    return RTA_OK;
+}
+
+} // namespace rta
+
+static void g_bounce_noalloc_limit_error(uint32_t nrays)
+{
+    char msg[160];
+    snprintf(msg, sizeof msg, "rta_diffuse_bounce_noalloc: %u rays exceed the %u-ray scratch", nrays,
+             (unsigned)RTA_BOUNCE_NOALLOC_MAX_RAYS);
+    rta::set_error_message(msg);
+}
+
+extern "C" int rta_diffuse_bounce_noalloc(const rta_lbvh *bvh, const float *orig, const float *dir,
+                                          const void *hits, uint32_t nrays, uint32_t seed, float eps,
+                                          float *out_orig, float *out_dir, float *out_maxt,
+                                          uint32_t *out_src, uint32_t *out_count, rta_stream_t stream)
+{
+    if (!bvh || !orig || !dir || !hits || !out_orig || !out_dir || !out_maxt || !out_src ||
+        !out_count || nrays == 0)
+        return RTA_ERR_INVALID;
+    if (nrays > RTA_BOUNCE_NOALLOC_MAX_RAYS) {
+        g_bounce_noalloc_limit_error(nrays);
+        return RTA_ERR_INVALID;
+    }
+    uint32_t *scratch = nullptr;
+    int rc = bounce_scratch(&scratch);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t tiles = (nrays + kBounceTile - 1) / kBounceTile;
+    // the tile counter, the count and the look-back words of this call start at zero
+    RTA_CUDA_TRY(cudaMemsetAsync(scratch, 0, (size_t)(4u + tiles) * 4u, s));
+    FrameState *fs = reinterpret_cast<FrameState *>(scratch);
+    k_bounce<<<tiles, kBounceThreads, 0, s>>>((const TriRec *)bvh->tris, orig, dir, (const HitRec *)hits,
+                                              nrays, seed, eps, out_orig, out_dir, out_maxt, out_src,
+                                              scratch + 4, fs, bvh->n);
+    if ((rc = check_launch("k_bounce (noalloc)"))) return rc;
+    RTA_CUDA_TRY(cudaMemcpyAsync(out_count, &fs->count, 4, cudaMemcpyDeviceToDevice, s));
+    return RTA_OK;
+}

@@ -24,8 +24,9 @@ SYMBOLS = [
     "rta_lbvh_reserve", "rta_lbvh_build", "rta_lbvh_get", "rta_lbvh_status", "rta_lbvh_to_2f4",
     "rta_trace", "rta_setup_shirley_rays", "rta_reset_intersections", "rta_frame_create",
     "rta_frame_destroy", "rta_frame_get", "rta_diffuse_bounce", "rta_frame_run",
-    "rta_frame_status",
+    "rta_frame_status", "rta_diffuse_bounce_noalloc",
 ]
+BOUNCE_NOALLOC_MAX_RAYS = 1 << 24
 
 
 class RtaError(RuntimeError):
@@ -77,6 +78,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_diffuse_bounce.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, u32, f32, vp]
     L.rta_frame_run.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, vp, u32, u32, f32, vp]
     L.rta_frame_status.argtypes = [vp, vp, P(u32)]
+    L.rta_diffuse_bounce_noalloc.argtypes = [P(LbvhView), vp, vp, vp, u32, u32, f32, vp, vp, vp, vp,
+                                             vp, vp]
     for name in SYMBOLS:
         fn = getattr(L, name)
         if fn.restype is None or fn.restype is C.c_int:
