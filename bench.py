@@ -42,8 +42,8 @@ SEED = 0
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--cpu-sample-rays", type=int, default=262144)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -85,6 +85,7 @@ class ClockSampler:
         self.rows = []
         self.proc = None
         self.thread = None
+        self.window = None
 
     def __enter__(self):
         q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -104,7 +105,14 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 7:
-                self.rows.append(parts)
+                self.rows.append((time.time(), parts))
+
+    def mark(self, start: bool):
+        """Brackets the timed region; only samples inside it are summarised."""
+        if start:
+            self.window = [time.time(), None]
+        else:
+            self.window[1] = time.time()
 
     def __exit__(self, *a):
         if self.proc:
@@ -115,14 +123,16 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if not self.rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        rows = [r for t, r in self.rows
+                if self.window is None or (self.window[0] <= t <= (self.window[1] or t))]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows)}
 
 
 # --------------------------------------------------------------------------- #
@@ -261,6 +271,7 @@ def run_gb300(args):
                                   P._ptr(rg.gpu_maxt), nrays, P._ptr(hits), L.TRACE_CIS, SEED,
                                   np.float32(1e-4), sh), "rta_frame_run")
 
+    clk = ClockSampler(local).__enter__()
     for _ in range(args.warmup):
         run_frame()
     torch.cuda.synchronize()
@@ -287,7 +298,9 @@ def run_gb300(args):
         pg.barrier()
     torch.cuda.synchronize()
     step_ms = []
-    with ClockSampler(local) as clk:
+    time.sleep(0.5)   # lets the clock sampler produce its first lines
+    clk.mark(True)
+    if True:
         for _ in range(args.steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -309,6 +322,8 @@ def run_gb300(args):
             e1.record()
             e1.synchronize()
             trace_ms.append(e0.elapsed_time(e1))
+    clk.mark(False)
+    clk.__exit__(None, None, None)
     if pg:
         pg.barrier()
     total_ms = max_over_ranks(sum(step_ms), pg, dev)
@@ -392,7 +407,11 @@ def run_gb300(args):
                   "frac_of_peak": 372 * n / (bmean * 1e-3) / 1e9 / peak},
         "trace": {"primary_ms": tr_ms, "primary_mrays_s": nrays / (tr_ms * 1e-3) / 1e6,
                   "inner_visits_per_ray": inner_visits / rays_per_step,
-                  "tri_tests_per_ray": tri_tests / rays_per_step},
+                  "tri_tests_per_ray": tri_tests / rays_per_step,
+                  "inner_visits_per_primary_ray": int(stp[0]) / nrays,
+                  "inner_visits_per_bounce_ray": int(stbs[0]) / max(nbounce, 1),
+                  "tri_tests_per_primary_ray": int(stp[1]) / nrays,
+                  "tri_tests_per_bounce_ray": int(stbs[1]) / max(nbounce, 1)},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

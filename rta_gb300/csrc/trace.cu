@@ -1,7 +1,8 @@
 // trace.cu -- binary-BVH traversal on sm_103a.
 //
-// Persistent warps pull batches of 32 rays from a global atomic queue; each
-// lane traverses one ray with a short stack in local memory (L1-resident).
+// Persistent warps pull rays from a global atomic queue; each lane traverses
+// one ray with a short stack in local memory (L1-resident), and idle lanes
+// refill from the queue while the rest of the warp is still busy.
 // The arithmetic is the reference's, operation for operation, through
 // explicit round-to-nearest intrinsics so no multiply-add is ever fused:
 //   slab test        intersect_aabb          (librta/intersect.h:56-150)
@@ -29,28 +30,50 @@ struct TraceArgs {
     uint32_t n_tris;    // bounds every link and triangle index before use
 };
 
-// intersect_aabb: per-axis division, zero-direction special case, early outs
-__device__ __forceinline__ bool slab_test(float lx, float hx, float ly, float hy, float lz, float hz,
-                                          const float o[3], const float d[3], float &dist)
+// Per-ray constants of the slab test: the ray and which direction components
+// are zero (intersect_aabb treats d == 0 separately).
+struct Ray {
+    float o[3], d[3];
+    uint32_t zero;   // bit k: d[k] == 0
+    float tmax;
+};
+
+__device__ __forceinline__ void make_ray(Ray &R, const float o[3], const float d[3], float tmax)
 {
-    float t_near = -FLT_MAX, t_far = FLT_MAX;
-    const float lo[3] = {lx, ly, lz}, hi[3] = {hx, hy, hz};
+    R.zero = 0;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        if (d[k] == 0.0f) {
-            if (o[k] < lo[k] || o[k] > hi[k]) return false;
+        R.o[k] = o[k];
+        R.d[k] = d[k];
+        if (d[k] == 0.0f) R.zero |= 1u << k;
+    }
+    R.tmax = tmax;
+}
+
+// intersect_aabb (librta/intersect.h:56-150).  The reference walks the axes
+// with early outs; t_near only grows and t_far only shrinks along the way, so
+// "no early out fired" equals "t_near <= t_far and t_far >= 0 at the end and
+// every zero-direction axis has the origin inside the slab".  The quotients
+// are the reference's correctly rounded (lo - o) / d.
+__device__ __forceinline__ bool slab_test(float lx, float hx, float ly, float hy, float lz, float hz,
+                                          const Ray &R, float &dist)
+{
+    const float lo[3] = {lx, ly, lz}, hi[3] = {hx, hy, hz};
+    float t_near = -FLT_MAX, t_far = FLT_MAX;
+    bool inside = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (R.zero & (1u << k)) {
+            inside = inside && !(R.o[k] < lo[k] || R.o[k] > hi[k]);
         } else {
-            float t1 = __fdiv_rn(__fsub_rn(lo[k], o[k]), d[k]);
-            float t2 = __fdiv_rn(__fsub_rn(hi[k], o[k]), d[k]);
-            if (t1 > t2) { float tmp = t1; t1 = t2; t2 = tmp; }
-            if (t1 > t_near) t_near = t1;
-            if (t2 < t_far) t_far = t2;
-            if (t_near > t_far) return false;
-            if (t_far < 0.0f) return false;
+            float t1 = __fdiv_rn(__fsub_rn(lo[k], R.o[k]), R.d[k]);
+            float t2 = __fdiv_rn(__fsub_rn(hi[k], R.o[k]), R.d[k]);
+            t_near = fmaxf(t_near, fminf(t1, t2));
+            t_far = fminf(t_far, fmaxf(t1, t2));
         }
     }
     dist = t_near;
-    return true;
+    return inside && t_near <= t_far && t_far >= 0.0f;
 }
 
 // intersect_aabb_aila with the ailabox kernels' reciprocal (kernels.cu:966-970)
@@ -71,7 +94,9 @@ __device__ __forceinline__ bool aila_test(float lx, float hx, float ly, float hy
     return near <= far && far >= 0.f && near < t;
 }
 
-// intersect_tri_opt, expression for expression
+// intersect_tri_opt, expression for expression.  A quotient x/M can only be
+// > 0 when x and M are non-zero with equal signs, so the three divisions are
+// skipped when that already fails (the result is a miss either way).
 __device__ __forceinline__ bool tri_test(const TriRec &T, const float o[3], const float dir[3],
                                          float &tt_out, float &beta_out, float &gamma_out)
 {
@@ -96,6 +121,11 @@ __device__ __forceinline__ bool tri_test(const TriRec &T, const float o[3], cons
     common3 = __fsub_rn(__fmul_rn(b, l), __fmul_rn(k, c));
     float gamma = __fadd_rn(__fadd_rn(__fmul_rn(i, common1), __fmul_rn(h, common2)), __fmul_rn(g, common3));
     float tt = -__fadd_rn(__fadd_rn(__fmul_rn(f, common1), __fmul_rn(e, common2)), __fmul_rn(d, common3));
+    const uint32_t sm = __float_as_uint(M) >> 31;
+    if (M == 0.0f || tt == 0.0f || beta == 0.0f || gamma == 0.0f ||
+        (__float_as_uint(tt) >> 31) != sm || (__float_as_uint(beta) >> 31) != sm ||
+        (__float_as_uint(gamma) >> 31) != sm)
+        return false;
     beta = __fdiv_rn(beta, M);
     gamma = __fdiv_rn(gamma, M);
     tt = __fdiv_rn(tt, M);
@@ -133,6 +163,12 @@ __device__ __forceinline__ TriRec load_tri(const TriRec *tris, uint32_t idx)
 
 // no ray visits more nodes than this; a corrupt tree ends the ray with a flag
 constexpr uint32_t kMaxSteps = 1u << 22;
+constexpr int kTraceThreads = 128;
+// idle lanes of a warp fetch new rays once at least this many are idle
+#ifndef RTA_FETCH_IDLE
+#define RTA_FETCH_IDLE 12
+#endif
+constexpr int kFetchIdle = RTA_FETCH_IDLE;
 
 struct Best {
     float t, beta, gamma;
@@ -168,144 +204,203 @@ __device__ __forceinline__ bool visit_leaf(const TriRec *tris, uint32_t n_tris, 
     return SHADOW && best.t != FLT_MAX;
 }
 
+// One lane = one ray at a time; each loop iteration visits one node.  Lanes
+// whose ray has finished take new rays from the global queue as soon as
+// kFetchIdle of them are idle, so warps stay full while the queue lasts.
 template <bool DIS, bool SHADOW, bool AILA, bool STATS, int STACK>
-__global__ void __launch_bounds__(128) k_trace(TraceArgs A)
+__global__ void __launch_bounds__(kTraceThreads) k_trace(TraceArgs A)
 {
     const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
     const uint32_t nrays = A.d_nrays ? *A.d_nrays : A.nrays;
     const RootRec root = *A.root;
+    const uint32_t n_inner = A.n_tris - 1u;
+
+    bool active = false, exhausted = false;
+    uint32_t r = 0, cur = 0, steps = 0, inner_visits = 0, tri_tests = 0;
+    int sp = -1;
+    uint32_t stack[STACK];
+    Ray R;
+    float id[3] = {0.f, 0.f, 0.f};
+    Best best;
+    float bx[6];   // DIS: box of the current node
+    bool overflow = false, capped = false, bad = false;
+
     for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(A.queue, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= nrays) break;
-        const uint32_t r = base + lane;
-        if (r >= nrays) continue;
-
-        float o[3], d[3];
-        o[0] = A.orig[3 * (size_t)r + 0];
-        o[1] = A.orig[3 * (size_t)r + 1];
-        o[2] = A.orig[3 * (size_t)r + 2];
-        d[0] = A.dir[3 * (size_t)r + 0];
-        d[1] = A.dir[3 * (size_t)r + 1];
-        d[2] = A.dir[3 * (size_t)r + 2];
-        const float tmax = A.maxt[r];
-        float id[3] = {0.f, 0.f, 0.f};
-        if (AILA) {
-            const float ooeps = 8.27180612553027674871e-25f;   // exp2f(-80)
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && __popc(idle) >= kFetchIdle) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(A.queue, (uint32_t)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base >= nrays) {
+                exhausted = true;
+            } else if (!active) {
+                r = base + __popc(idle & lt_mask);
+                if (r < nrays) {
+                    float o[3], d[3];
+                    o[0] = A.orig[3 * (size_t)r + 0];
+                    o[1] = A.orig[3 * (size_t)r + 1];
+                    o[2] = A.orig[3 * (size_t)r + 2];
+                    d[0] = A.dir[3 * (size_t)r + 0];
+                    d[1] = A.dir[3 * (size_t)r + 1];
+                    d[2] = A.dir[3 * (size_t)r + 2];
+                    make_ray(R, o, d, A.maxt[r]);
+                    if (AILA) {
+                        const float ooeps = 8.27180612553027674871e-25f;   // exp2f(-80)
 #pragma unroll
-            for (int k = 0; k < 3; ++k)
-                id[k] = __fdiv_rn(1.0f, fabsf(d[k]) > ooeps ? d[k] : copysignf(ooeps, d[k]));
+                        for (int k = 0; k < 3; ++k)
+                            id[k] = __fdiv_rn(1.0f, fabsf(d[k]) > ooeps ? d[k] : copysignf(ooeps, d[k]));
+                    }
+                    best.t = FLT_MAX;
+                    best.beta = best.gamma = 0.f;
+                    best.ref = 0;
+                    sp = -1;
+                    steps = inner_visits = tri_tests = 0;
+                    cur = root.link;
+                    if (DIS) {
+                        bx[0] = root.lo[0]; bx[1] = root.hi[0]; bx[2] = root.lo[1];
+                        bx[3] = root.hi[1]; bx[4] = root.lo[2]; bx[5] = root.hi[2];
+                    }
+                    active = true;
+                }
+            }
         }
-        Best best;
-        best.t = FLT_MAX;
-        best.beta = best.gamma = 0.f;
-        best.ref = 0;
-        uint32_t stack[STACK];
-        int sp = -1;
-        uint32_t inner_visits = 0, tri_tests = 0;
-        bool overflow = false, capped = false, bad = false;
-        const uint32_t n_inner = A.n_tris - 1u;
+        if (!__any_sync(0xffffffffu, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (!active) continue;
 
-        if (!DIS) {
-            // child-is: the current node's children are tested together
-            uint32_t cur = root.link;
-            for (uint32_t steps = 0;; ++steps) {
-                if (steps >= kMaxSteps) { capped = true; break; }
-                if (!is_leaf(cur)) {
-                    if (cur >= n_inner) { bad = true; break; }
+        // ---- one traversal step ----
+        bool done = false;
+        if (++steps > kMaxSteps) {
+            capped = true;
+            done = true;
+        } else if (!DIS) {
+            // child-is (kernels.cu:797-852): test both children, nearer first
+            if (!is_leaf(cur)) {
+                if (cur >= n_inner) {
+                    bad = true;
+                    done = true;
+                } else {
                     ++inner_visits;
                     const NodeRec nd = load_node(A.nodes, cur);
                     float dl = FLT_MAX, dr = FLT_MAX;
                     bool hl, hr;
                     if (AILA) {
-                        hl = aila_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, o, id, best.t, dl);
-                        hr = aila_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, o, id, best.t, dr);
+                        hl = aila_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R.o, id, best.t, dl);
+                        hr = aila_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R.o, id, best.t, dr);
                     } else {
-                        hl = slab_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, o, d, dl);
-                        hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, o, d, dr);
+                        hl = slab_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, dl);
+                        hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, dr);
                     }
-                    if (dl >= best.t || dl > tmax) hl = false;
-                    if (dr >= best.t || dr > tmax) hr = false;
+                    if (dl >= best.t || dl > R.tmax) hl = false;
+                    if (dr >= best.t || dr > R.tmax) hr = false;
+                    const bool left_first = dl <= dr;
                     if (hl && hr) {
-                        if (sp + 1 >= STACK) { overflow = true; break; }
-                        if (dl <= dr) { stack[++sp] = nd.q3.y; cur = nd.q3.x; }
-                        else { stack[++sp] = nd.q3.x; cur = nd.q3.y; }
+                        if (sp + 1 >= STACK) {
+                            overflow = true;
+                            done = true;
+                        } else if (left_first) {
+                            stack[++sp] = nd.q3.y;
+                            cur = nd.q3.x;
+                        } else {
+                            stack[++sp] = nd.q3.x;
+                            cur = nd.q3.y;
+                        }
                     } else if (hl) {
                         cur = nd.q3.x;
                     } else if (hr) {
                         cur = nd.q3.y;
+                    } else if (sp < 0) {
+                        done = true;
                     } else {
-                        if (sp < 0) break;
                         cur = stack[sp--];
                     }
-                } else {
-                    if (visit_leaf<SHADOW>(A.tris, A.n_tris, cur, o, d, tmax, best, tri_tests, bad)) break;
-                    if (sp < 0) break;
-                    cur = stack[sp--];
                 }
+            } else {
+                if (visit_leaf<SHADOW>(A.tris, A.n_tris, cur, R.o, R.d, R.tmax, best, tri_tests, bad))
+                    done = true;
+                else if (sp < 0)
+                    done = true;
+                else
+                    cur = stack[sp--];
             }
         } else {
-            // direct-is: a node's own box is tested when it is visited; the
-            // stack holds (parent << 1 | side) so a popped node's box is re-read
-            // from its parent's record
-            uint32_t cur = root.link;
-            float bx[6] = {root.lo[0], root.hi[0], root.lo[1], root.hi[1], root.lo[2], root.hi[2]};
-            float dist = FLT_MAX;
-            for (uint32_t steps = 0;; ++steps) {
-                if (steps >= kMaxSteps) { capped = true; break; }
-                bool pop = false;
-                if (!is_leaf(cur)) {
-                    ++inner_visits;
-                    bool h = AILA ? aila_test(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], o, id, best.t, dist)
-                                  : slab_test(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], o, d, dist);
-                    if (dist >= best.t || dist > tmax) h = false;
-                    if (h) {
-                        if (sp + 1 >= STACK) { overflow = true; break; }
-                        if (cur >= n_inner) { bad = true; break; }
+            // direct-is (kernels.cu:506-545): a node's own box is tested when it
+            // is visited; the stack holds (parent << 1 | side) and a popped
+            // node's box is re-read from its parent's record
+            bool pop = false;
+            if (!is_leaf(cur)) {
+                ++inner_visits;
+                float dist = FLT_MAX;
+                bool h = AILA ? aila_test(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], R.o, id, best.t, dist)
+                              : slab_test(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], R, dist);
+                if (dist >= best.t || dist > R.tmax) h = false;
+                if (h) {
+                    if (sp + 1 >= STACK) {
+                        overflow = true;
+                        done = true;
+                    } else if (cur >= n_inner) {
+                        bad = true;
+                        done = true;
+                    } else {
                         const NodeRec nd = load_node(A.nodes, cur);
                         stack[++sp] = (cur << 1) | 1u;
                         cur = nd.q3.x;
                         bx[0] = nd.q0.x; bx[1] = nd.q0.y; bx[2] = nd.q0.z;
                         bx[3] = nd.q0.w; bx[4] = nd.q1.x; bx[5] = nd.q1.y;
-                    } else {
-                        pop = true;
                     }
                 } else {
-                    if (visit_leaf<SHADOW>(A.tris, A.n_tris, cur, o, d, tmax, best, tri_tests, bad)) break;
                     pop = true;
                 }
-                if (pop) {
-                    if (sp < 0) break;
+            } else {
+                if (visit_leaf<SHADOW>(A.tris, A.n_tris, cur, R.o, R.d, R.tmax, best, tri_tests, bad))
+                    done = true;
+                else
+                    pop = true;
+            }
+            if (pop && !done) {
+                if (sp < 0) {
+                    done = true;
+                } else {
                     const uint32_t e = stack[sp--];
-                    if ((e >> 1) >= n_inner) { bad = true; break; }
-                    const NodeRec nd = load_node(A.nodes, e >> 1);
-                    if (e & 1u) {
-                        cur = nd.q3.y;
-                        bx[0] = nd.q1.z; bx[1] = nd.q1.w; bx[2] = nd.q2.x;
-                        bx[3] = nd.q2.y; bx[4] = nd.q2.z; bx[5] = nd.q2.w;
+                    if ((e >> 1) >= n_inner) {
+                        bad = true;
+                        done = true;
                     } else {
-                        cur = nd.q3.x;
-                        bx[0] = nd.q0.x; bx[1] = nd.q0.y; bx[2] = nd.q0.z;
-                        bx[3] = nd.q0.w; bx[4] = nd.q1.x; bx[5] = nd.q1.y;
+                        const NodeRec nd = load_node(A.nodes, e >> 1);
+                        if (e & 1u) {
+                            cur = nd.q3.y;
+                            bx[0] = nd.q1.z; bx[1] = nd.q1.w; bx[2] = nd.q2.x;
+                            bx[3] = nd.q2.y; bx[4] = nd.q2.z; bx[5] = nd.q2.w;
+                        } else {
+                            cur = nd.q3.x;
+                            bx[0] = nd.q0.x; bx[1] = nd.q0.y; bx[2] = nd.q0.z;
+                            bx[3] = nd.q0.w; bx[4] = nd.q1.x; bx[5] = nd.q1.y;
+                        }
                     }
                 }
             }
         }
-        if (overflow) atomicOr(A.status, RTA_DEV_STACK_OVERFLOW);
-        if (capped) atomicOr(A.status, RTA_DEV_ITER_LIMIT);
-        if (bad) atomicOr(A.status, RTA_DEV_BAD_LINK);
-        if (best.t != FLT_MAX) {
-            reinterpret_cast<float4 *>(A.hits)[r] =
-                make_float4(best.t, best.beta, best.gamma, __uint_as_float(best.ref));
-        } else {
-            A.hits[r].t = FLT_MAX;
-        }
-        if (STATS) {
-            A.stats[2 * (size_t)r + 0] = inner_visits;
-            A.stats[2 * (size_t)r + 1] = tri_tests;
+        if (done) {
+            if (best.t != FLT_MAX) {
+                reinterpret_cast<float4 *>(A.hits)[r] =
+                    make_float4(best.t, best.beta, best.gamma, __uint_as_float(best.ref));
+            } else {
+                A.hits[r].t = FLT_MAX;
+            }
+            if (STATS) {
+                A.stats[2 * (size_t)r + 0] = inner_visits;
+                A.stats[2 * (size_t)r + 1] = tri_tests;
+            }
+            active = false;
         }
     }
+    if (overflow) atomicOr(A.status, RTA_DEV_STACK_OVERFLOW);
+    if (capped) atomicOr(A.status, RTA_DEV_ITER_LIMIT);
+    if (bad) atomicOr(A.status, RTA_DEV_BAD_LINK);
 }
 
 template <bool DIS, bool SHADOW, bool AILA, bool STATS, int STACK>
@@ -314,12 +409,12 @@ static int launch_trace(const TraceArgs &a, cudaStream_t s)
     static int blocks = 0;
     if (!blocks) {
         int per_sm = 0, dev = 0, sms = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<DIS, SHADOW, AILA, STATS, STACK>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<DIS, SHADOW, AILA, STATS, STACK>, kTraceThreads, 0);
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
     }
-    k_trace<DIS, SHADOW, AILA, STATS, STACK><<<blocks, 128, 0, s>>>(a);
+    k_trace<DIS, SHADOW, AILA, STATS, STACK><<<blocks, kTraceThreads, 0, s>>>(a);
     return check_launch("k_trace");
 }
 

@@ -51,8 +51,9 @@ _lib = None
 
 
 def load(path: str = LIB_PATH) -> C.CDLL:
+    """The library at `path` with its argument types declared (cached)."""
     global _lib
-    if _lib is not None:
+    if _lib is not None and path == LIB_PATH:
         return _lib
     if not os.path.exists(path):
         raise RtaError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; "
@@ -81,11 +82,14 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_diffuse_bounce_noalloc.argtypes = [P(LbvhView), vp, vp, vp, u32, u32, f32, vp, vp, vp, vp,
                                              vp, vp]
     for name in SYMBOLS:
+        if not hasattr(L, name):
+            continue
         fn = getattr(L, name)
         if fn.restype is None or fn.restype is C.c_int:
             if name not in ("rta_last_error", "rta_lbvh_max_triangles"):
                 fn.restype = C.c_int
-    _lib = L
+    if path == LIB_PATH:
+        _lib = L
     return L
 
 
