@@ -197,6 +197,52 @@ int rta_diffuse_bounce_noalloc(const rta_lbvh *bvh, const float *orig, const flo
                                float *out_orig, float *out_dir, float *out_maxt, uint32_t *out_src,
                                uint32_t *out_count, rta_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* learned child order (no reference counterpart): a 14-32-32-1 network      */
+/* that picks which child to visit first where the child-is traversal hits   */
+/* both children; trained on decisions recorded from the plain traversal     */
+/* ------------------------------------------------------------------------ */
+
+typedef struct rta_order_model rta_order_model;
+
+/* Network (Glorot-uniform from `seed`), optimiser state and room for
+ * max_samples training samples (64 bytes each on the device). */
+int rta_order_create(rta_order_model **model, uint32_t max_samples, uint32_t seed);
+int rta_order_destroy(rta_order_model *model);
+/* number of network parameters: w1 (32x16), b1, w2 (32x32), b2, w3, b3 as fp32 */
+uint32_t rta_order_param_count(void);
+int rta_order_get_params(const rta_order_model *model, float *host_params);
+int rta_order_set_params(rta_order_model *model, const float *host_params);
+
+/* Plain child-is closest-hit trace (as rta_trace with RTA_TRACE_CIS) that
+ * also records every node where both children are hit and not culled, then
+ * labels those samples from the final hits; successive calls append until
+ * max_samples are held. */
+int rta_order_sample(rta_order_model *model, const rta_lbvh *bvh, const float *orig,
+                     const float *dir, const float *maxt, uint32_t nrays, const uint32_t *d_nrays,
+                     void *hits, rta_stream_t stream);
+int rta_order_sample_count(const rta_order_model *model, uint32_t *count);
+int rta_order_clear_samples(rta_order_model *model);
+/* device pointer to the sample records (for inspection) */
+int rta_order_samples(const rta_order_model *model, void **d_samples);
+
+/* Gradient of the mean weighted binary cross-entropy over samples
+ * [first, first+count) at the current parameters; no update. */
+int rta_order_gradient(rta_order_model *model, uint32_t first, uint32_t count, float *host_grad,
+                       float *host_loss);
+/* Adam over the held samples, `epochs` passes of minibatches of `batch`. */
+int rta_order_train(rta_order_model *model, uint32_t epochs, uint32_t batch, float lr,
+                    float *last_loss, rta_stream_t stream);
+
+/* Child-is closest-hit trace whose two-child order comes from the network.
+ * Every child hit closer than the current t is still visited, so each ray's
+ * closest hit is the plain order's, except that of two triangles hit at
+ * exactly the same t another one may be found first.  stats as in rta_trace
+ * (nullable). */
+int rta_trace_learned(const rta_lbvh *bvh, const rta_order_model *model, const float *orig,
+                      const float *dir, const float *maxt, uint32_t nrays, const uint32_t *d_nrays,
+                      void *hits, uint32_t *stats, rta_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

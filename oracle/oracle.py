@@ -186,3 +186,78 @@ def bbvh_trace_cis(nodes, tris, orig, dirs, maxt, threads=0):
     lib().orc_bbvh_trace_cis(_p(nodes), _p(tris), _p(orig), _p(dirs), _p(maxt), nr, _p(hits),
                              threads)
     return hits
+
+
+# --------------------------------------------------------------------------- #
+# child-order network (checker of the tensor-core training kernels)            #
+# --------------------------------------------------------------------------- #
+
+MLP_PARAMS = 32 * 16 + 32 + 32 * 32 + 32 + 32 + 1
+SAMPLE_DTYPE = np.dtype([("x", "<u2", 16), ("ray", "<u4"), ("lfirst", "<u4"), ("lsize", "<u4"),
+                         ("rfirst", "<u4"), ("rsize", "<u4"), ("label", "<f4"), ("weight", "<f4"),
+                         ("pad", "<u4")])
+
+
+def bf16_round(x: np.ndarray) -> np.ndarray:
+    """float32 -> nearest bfloat16 (ties to even) -> float32."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def bf16_bits_to_f32(b: np.ndarray) -> np.ndarray:
+    return (np.asarray(b, np.uint32) << 16).view(np.float32)
+
+
+def mlp_unpack(params):
+    p = np.asarray(params, np.float64)
+    o = 0
+    w1 = p[o:o + 512].reshape(32, 16); o += 512
+    b1 = p[o:o + 32]; o += 32
+    w2 = p[o:o + 1024].reshape(32, 32); o += 1024
+    b2 = p[o:o + 32]; o += 32
+    w3 = p[o:o + 32]; o += 32
+    b3 = p[o]
+    return w1, b1, w2, b2, w3, b3
+
+
+def mlp_logits(params, x):
+    """Forward pass with the kernels' rounding points: bf16 weights, inputs
+    and hidden activations, accumulation in (here: double) precision."""
+    w1, b1, w2, b2, w3, b3 = mlp_unpack(params)
+    r = lambda a: bf16_round(np.asarray(a, np.float32)).astype(np.float64)  # noqa: E731
+    z1 = r(x) @ r(w1).T + b1
+    h1 = r(np.maximum(z1, 0))
+    z2 = h1 @ r(w2).T + b2
+    h2 = r(np.maximum(z2, 0))
+    return h2 @ r(w3) + b3
+
+
+def mlp_gradient(params, x, label, weight, scale):
+    """Gradient of scale * sum(weight * BCE(logit, label)) and the weighted
+    loss sum, restating k_mlp_grad (rta_gb300/csrc/learn.cu) in float64."""
+    w1, b1, w2, b2, w3, b3 = mlp_unpack(params)
+    r = lambda a: bf16_round(np.asarray(a, np.float32)).astype(np.float64)  # noqa: E731
+    x = r(x)
+    label = np.asarray(label, np.float64)
+    weight = np.asarray(weight, np.float64)
+    z1 = x @ r(w1).T + b1
+    h1 = r(np.maximum(z1, 0))
+    z2 = h1 @ r(w2).T + b2
+    h2 = r(np.maximum(z2, 0))
+    y = h2 @ r(w3) + b3
+    p = 1.0 / (1.0 + np.exp(-y))
+    dy = (p - label) * weight * scale
+    loss = float(np.sum(weight * (np.maximum(y, 0) - y * label + np.log1p(np.exp(-np.abs(y))))))
+    g_b3 = dy.sum()
+    g_w3 = dy @ h2
+    dz2 = (z2 > 0) * (dy[:, None] * r(w3)[None, :])
+    g_b2 = dz2.sum(0)
+    dz2b = r(dz2)
+    g_w2 = dz2b.T @ h1
+    dh1 = dz2b @ r(w2)
+    dz1 = (z1 > 0) * dh1
+    g_b1 = dz1.sum(0)
+    g_w1 = r(dz1).T @ x
+    grad = np.concatenate([g_w1.ravel(), g_b1, g_w2.ravel(), g_b2, g_w3, [g_b3]])
+    return grad, loss

@@ -417,7 +417,7 @@ __device__ __forceinline__ int cpl(const Key *__restrict__ codes, int n, int i, 
 
 template <typename Key>
 __device__ __forceinline__ void karras_split(const Key *__restrict__ codes, int n, int i, int &left,
-                                             int &right)
+                                             int &right, int &left_size, int &right_size)
 {
     // build_tree_karras (:205-249): direction, range end (exponential +
     // binary search), split (binary search with ceiling halving)
@@ -442,6 +442,8 @@ __device__ __forceinline__ void karras_split(const Key *__restrict__ codes, int 
     int mid = from + s;
     left = (from == mid) ? mid + n - 1 : mid;
     right = (to == mid + 1) ? mid + 1 + n - 1 : mid + 1;
+    left_size = mid - from + 1;
+    right_size = to - mid;
 }
 
 template <typename Key>
@@ -453,12 +455,12 @@ k_karras(const Key *__restrict__ codes, const uint32_t *__restrict__ ids, uint32
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (i + 1 < n) {
-        int l, r;
-        karras_split(codes, (int)n, (int)i, l, r);
+        int l, r, ls, rs;
+        karras_split(codes, (int)n, (int)i, l, r, ls, rs);
         const uint32_t inner = n - 1;
         uint32_t llink = (uint32_t)l < inner ? (uint32_t)l : make_leaf((uint32_t)l - inner, 1u);
         uint32_t rlink = (uint32_t)r < inner ? (uint32_t)r : make_leaf((uint32_t)r - inner, 1u);
-        nodes[i].q3 = make_uint4(llink, rlink, (uint32_t)l, (uint32_t)r);
+        nodes[i].q3 = make_uint4(llink, rlink, (uint32_t)ls, (uint32_t)rs);
         parents[l] = (i << 1) | 0u;
         parents[r] = (i << 1) | 1u;
         counters[i] = 0u;
@@ -638,9 +640,15 @@ __global__ void k_to_2f4(const NodeRec *__restrict__ nodes, const RootRec *__res
         w0 = cnt << 1;
         w1 = leaf_first(link);
     } else {
+        // reference numbering of the children: an inner link is the node
+        // index; a leaf link (first, count) is leaf n-1+first if count is 1,
+        // else a collapsed inner node, which is its range's end for a left
+        // child and its range's start for a right child
         const uint4 q = nodes[k].q3;
-        w0 = (q.z << 1) | 1u;
-        w1 = q.w;
+        const uint32_t l = !is_leaf(q.x) ? q.x : (q.z == 1u ? n - 1 + leaf_first(q.x) : leaf_first(q.x) + q.z - 1u);
+        const uint32_t r = !is_leaf(q.y) ? q.y : (q.w == 1u ? n - 1 + leaf_first(q.y) : leaf_first(q.y));
+        w0 = (l << 1) | 1u;
+        w1 = r;
     }
     out[2 * k + 0] = make_float4(__uint_as_float(w0), __uint_as_float(w1), lo[0], lo[1]);
     out[2 * k + 1] = make_float4(lo[2], hi[0], hi[1], hi[2]);

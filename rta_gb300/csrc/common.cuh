@@ -9,9 +9,11 @@
 //              q0 = left  (lo.x, hi.x, lo.y, hi.y)
 //              q1 = left  (lo.z, hi.z), right (lo.x, hi.x)
 //              q2 = right (lo.y, hi.y, lo.z, hi.z)
-//              q3 = (left link, right link, left ref-index, right ref-index)
-//            The ref-index words keep the reference's node numbering of the
-//            children so the tree can be written out in its 2F4 layout.
+//              q3 = (left link, right link, left size, right size)
+//            size = number of triangles under the child (its Morton range).
+//            A left child's range ends at its node index and a right child's
+//            range starts at it (Karras' split), so the reference's node
+//            numbering of every child follows from link and size.
 //   RootRec  32 B: root box and root link.
 //   TriRec   48 B per triangle in Morton order: (a, count), (b, id), (c, 0).
 //            count = number of triangles of the leaf that starts here.

@@ -13,6 +13,7 @@
 //   DIS  trace_dis(float4*)  (bbvh-cuda/kernels.cu:486-548)
 // so hits, including which of two equal-t triangles wins, are the reference's.
 #include "common.cuh"
+#include "mlp.cuh"
 
 namespace rta {
 
@@ -56,7 +57,7 @@ __device__ __forceinline__ void make_ray(Ray &R, const float o[3], const float d
 // every zero-direction axis has the origin inside the slab".  The quotients
 // are the reference's correctly rounded (lo - o) / d.
 __device__ __forceinline__ bool slab_test(float lx, float hx, float ly, float hy, float lz, float hz,
-                                          const Ray &R, float &dist)
+                                          const Ray &R, float &dist, float &far)
 {
     const float lo[3] = {lx, ly, lz}, hi[3] = {hx, hy, hz};
     float t_near = -FLT_MAX, t_far = FLT_MAX;
@@ -73,7 +74,15 @@ __device__ __forceinline__ bool slab_test(float lx, float hx, float ly, float hy
         }
     }
     dist = t_near;
+    far = t_far;
     return inside && t_near <= t_far && t_far >= 0.0f;
+}
+
+__device__ __forceinline__ bool slab_test(float lx, float hx, float ly, float hy, float lz, float hz,
+                                          const Ray &R, float &dist)
+{
+    float far;
+    return slab_test(lx, hx, ly, hy, lz, hz, R, dist, far);
 }
 
 // intersect_aabb_aila with the ailabox kernels' reciprocal (kernels.cu:966-970)
@@ -401,6 +410,284 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(TraceArgs A)
     if (overflow) atomicOr(A.status, RTA_DEV_STACK_OVERFLOW);
     if (capped) atomicOr(A.status, RTA_DEV_ITER_LIMIT);
     if (bad) atomicOr(A.status, RTA_DEV_BAD_LINK);
+}
+
+// ------------------------------------------------------------------------- //
+// child-is traversal with a learned child order, and its sample recorder     //
+// ------------------------------------------------------------------------- //
+//
+// The plain order visits the child with the smaller entry distance first
+// (kernels.cu:818-827).  LEARNED asks the network instead at every node
+// where both children are hit and not culled; every such child is still
+// visited, so the closest hit is the same (up to which of two triangles at
+// exactly the same t is found first).  SAMPLE keeps the plain order and
+// records each such decision for training.  Lanes converge once per step so
+// that the warp evaluates the network for all deciding lanes at once on the
+// tensor cores.
+
+struct LearnArgs {
+    TraceArgs t;
+    const MlpWeights *w;
+    Sample *samples;
+    uint32_t *sample_count;
+    uint32_t sample_cap;
+};
+
+__device__ __forceinline__ float clampf4(float v) { return fminf(fmaxf(v, -4.0f), 4.0f); }
+
+template <bool SAMPLE, bool LEARNED, bool STATS, int STACK>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
+{
+    const TraceArgs &A = L.t;
+    __shared__ MlpWeights sw;
+    __shared__ __align__(16) __nv_bfloat16 xs[kTraceThreads / 32][32][kMlpIn];
+    if (LEARNED) {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(L.w);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&sw);
+        for (int i = threadIdx.x; i < (int)(sizeof(MlpWeights) / 4); i += blockDim.x) dst[i] = src[i];
+        __syncthreads();
+    }
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const uint32_t nrays = A.d_nrays ? *A.d_nrays : A.nrays;
+    const RootRec root = *A.root;
+    const uint32_t n_inner = A.n_tris - 1u;
+
+    bool active = false, exhausted = false;
+    uint32_t r = 0, cur = 0, depth = 0, steps = 0, inner_visits = 0, tri_tests = 0;
+    int sp = -1;
+    uint32_t stack[STACK];
+    Ray R;
+    Best best;
+    bool overflow = false, capped = false, bad = false;
+
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && __popc(idle) >= kFetchIdle) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(A.queue, (uint32_t)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base >= nrays) {
+                exhausted = true;
+            } else if (!active) {
+                r = base + __popc(idle & lt_mask);
+                if (r < nrays) {
+                    float o[3], d[3];
+                    for (int k = 0; k < 3; ++k) {
+                        o[k] = A.orig[3 * (size_t)r + k];
+                        d[k] = A.dir[3 * (size_t)r + k];
+                    }
+                    make_ray(R, o, d, A.maxt[r]);
+                    best.t = FLT_MAX;
+                    best.beta = best.gamma = 0.f;
+                    best.ref = 0;
+                    sp = -1;
+                    steps = inner_visits = tri_tests = depth = 0;
+                    cur = root.link;
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (exhausted) break;
+            continue;
+        }
+
+        bool done = false, at_inner = false, need = false, hl = false, hr = false;
+        NodeRec nd;
+        float tnl = FLT_MAX, tfl = FLT_MAX, tnr = FLT_MAX, tfr = FLT_MAX;
+        if (active) {
+            if (++steps > kMaxSteps) {
+                capped = true;
+                done = true;
+            } else if (!is_leaf(cur)) {
+                if (cur >= n_inner) {
+                    bad = true;
+                    done = true;
+                } else {
+                    at_inner = true;
+                    ++inner_visits;
+                    nd = load_node(A.nodes, cur);
+                    hl = slab_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, tnl, tfl);
+                    hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, tnr, tfr);
+                    if (tnl >= best.t || tnl > R.tmax) hl = false;
+                    if (tnr >= best.t || tnr > R.tmax) hr = false;
+                    need = hl && hr;
+                }
+            }
+        }
+        bool left_first = tnl <= tnr;
+        if (SAMPLE || LEARNED) {
+            float x[kMlpIn];
+            if (need) {
+                const float base = fminf(tnl, tnr), span = fmaxf(tfl, tfr) - base;
+                const float inv = span > 0.0f ? 1.0f / span : 0.0f;
+                x[0] = clampf4(R.d[0]);
+                x[1] = clampf4(R.d[1]);
+                x[2] = clampf4(R.d[2]);
+                x[3] = clampf4((tnl - base) * inv);
+                x[4] = clampf4((tfl - base) * inv);
+                x[5] = clampf4((tnr - base) * inv);
+                x[6] = clampf4((tfr - base) * inv);
+                x[7] = (float)depth * (1.0f / 32.0f);
+                x[8] = log2f((float)nd.q3.z) * (1.0f / 25.0f);
+                x[9] = log2f((float)nd.q3.w) * (1.0f / 25.0f);
+                x[10] = best.t != FLT_MAX ? 1.0f : 0.0f;
+                x[11] = best.t != FLT_MAX ? clampf4((best.t - base) * inv) * 0.25f : 1.0f;
+                x[12] = (is_leaf(nd.q3.x) ? 1.0f : 0.0f) - (is_leaf(nd.q3.y) ? 1.0f : 0.0f);
+                x[13] = tnl <= tnr ? 1.0f : -1.0f;
+                x[14] = x[15] = 0.0f;
+            } else {
+#pragma unroll
+                for (int k = 0; k < kMlpIn; ++k) x[k] = 0.0f;
+            }
+            if (SAMPLE) {
+                const uint32_t m = __ballot_sync(0xffffffffu, need);
+                if (m) {
+                    const int leader = __ffs(m) - 1;
+                    uint32_t base = 0;
+                    if ((int)lane == leader) base = atomicAdd(L.sample_count, (uint32_t)__popc(m));
+                    base = __shfl_sync(0xffffffffu, base, leader);
+                    const uint32_t idx = base + __popc(m & lt_mask);
+                    if (need && idx < L.sample_cap) {
+                        Sample smp;
+#pragma unroll
+                        for (int k = 0; k < kMlpIn; ++k) smp.x[k] = __float2bfloat16_rn(x[k]);
+                        smp.ray = r;
+                        smp.lsize = nd.q3.z;
+                        smp.rsize = nd.q3.w;
+                        smp.lfirst = is_leaf(nd.q3.x) ? leaf_first(nd.q3.x) : nd.q3.x - nd.q3.z + 1u;
+                        smp.rfirst = is_leaf(nd.q3.y) ? leaf_first(nd.q3.y) : nd.q3.y;
+                        smp.label = 0.f;
+                        smp.weight = 0.f;
+                        smp.pad = 0;
+                        L.samples[idx] = smp;
+                    }
+                }
+            }
+            if (LEARNED) {
+                if (__any_sync(0xffffffffu, need)) {
+#pragma unroll
+                    for (int k = 0; k < kMlpIn; k += 2)
+                        *reinterpret_cast<uint32_t *>(&xs[warp][lane][k]) = pack_bf16(x[k], x[k + 1]);
+                    __syncwarp();
+                    MlpForward F;
+                    mlp_forward(sw, xs[warp], F);
+                    const float logit = mlp_own_logit(F);
+                    __syncwarp();
+                    if (need) left_first = logit > 0.0f;
+                }
+            }
+        }
+        if (active && !done) {
+            if (at_inner) {
+                if (hl && hr) {
+                    if (sp + 1 >= STACK) {
+                        overflow = true;
+                        done = true;
+                    } else {
+                        const uint32_t far = left_first ? nd.q3.y : nd.q3.x;
+                        const uint32_t d1 = depth + 1u < 63u ? depth + 1u : 63u;
+                        stack[++sp] = is_leaf(far) ? far : (far | (d1 << kCountShift));
+                        cur = left_first ? nd.q3.x : nd.q3.y;
+                        depth = d1;
+                    }
+                } else if (hl) {
+                    cur = nd.q3.x;
+                    depth = depth + 1u < 63u ? depth + 1u : 63u;
+                } else if (hr) {
+                    cur = nd.q3.y;
+                    depth = depth + 1u < 63u ? depth + 1u : 63u;
+                } else if (sp < 0) {
+                    done = true;
+                } else {
+                    const uint32_t e = stack[sp--];
+                    cur = is_leaf(e) ? e : (e & kFirstMask);
+                    if (!is_leaf(e)) depth = (e >> kCountShift) & kCountMask;
+                }
+            } else {
+                if (visit_leaf<false>(A.tris, A.n_tris, cur, R.o, R.d, R.tmax, best, tri_tests, bad))
+                    done = true;
+                else if (sp < 0)
+                    done = true;
+                else {
+                    const uint32_t e = stack[sp--];
+                    cur = is_leaf(e) ? e : (e & kFirstMask);
+                    if (!is_leaf(e)) depth = (e >> kCountShift) & kCountMask;
+                }
+            }
+        }
+        if (done) {
+            if (best.t != FLT_MAX) {
+                reinterpret_cast<float4 *>(A.hits)[r] =
+                    make_float4(best.t, best.beta, best.gamma, __uint_as_float(best.ref));
+            } else {
+                A.hits[r].t = FLT_MAX;
+            }
+            if (STATS) {
+                A.stats[2 * (size_t)r + 0] = inner_visits;
+                A.stats[2 * (size_t)r + 1] = tri_tests;
+            }
+            active = false;
+        }
+    }
+    if (overflow) atomicOr(A.status, RTA_DEV_STACK_OVERFLOW);
+    if (capped) atomicOr(A.status, RTA_DEV_ITER_LIMIT);
+    if (bad) atomicOr(A.status, RTA_DEV_BAD_LINK);
+}
+
+template <bool SAMPLE, bool LEARNED, bool STATS, int STACK>
+static int launch_learn(const LearnArgs &a, cudaStream_t s)
+{
+    static int blocks = 0;
+    if (!blocks) {
+        int per_sm = 0, dev = 0, sms = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_learn<SAMPLE, LEARNED, STATS, STACK>,
+                                                      kTraceThreads, 0);
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    }
+    k_trace_learn<SAMPLE, LEARNED, STATS, STACK><<<blocks, kTraceThreads, 0, s>>>(a);
+    return check_launch("k_trace_learn");
+}
+
+template <int STACK>
+static int dispatch_learn(const LearnArgs &a, bool sample, bool learned, bool stats, cudaStream_t s)
+{
+    if (sample) return launch_learn<true, false, false, STACK>(a, s);
+    if (learned) return stats ? launch_learn<false, true, true, STACK>(a, s) : launch_learn<false, true, false, STACK>(a, s);
+    return stats ? launch_learn<false, false, true, STACK>(a, s) : launch_learn<false, false, false, STACK>(a, s);
+}
+
+int trace_learn_impl(const rta_lbvh *bvh, const MlpWeights *w, const float *orig, const float *dir,
+                     const float *maxt, uint32_t nrays, const uint32_t *d_nrays, void *hits,
+                     uint32_t *stats, Sample *samples, uint32_t *sample_count, uint32_t sample_cap,
+                     uint32_t *queue, bool learned, cudaStream_t s)
+{
+    LearnArgs a;
+    a.t.nodes = (const NodeRec *)bvh->nodes;
+    a.t.root = (const RootRec *)bvh->root;
+    a.t.tris = (const TriRec *)bvh->tris;
+    a.t.orig = orig;
+    a.t.dir = dir;
+    a.t.maxt = maxt;
+    a.t.nrays = nrays;
+    a.t.d_nrays = d_nrays;
+    a.t.hits = (HitRec *)hits;
+    a.t.stats = stats;
+    a.t.queue = queue;
+    a.t.status = bvh->status;
+    a.t.n_tris = bvh->n;
+    a.w = w;
+    a.samples = samples;
+    a.sample_count = sample_count;
+    a.sample_cap = sample_cap;
+    RTA_CUDA_TRY(cudaMemsetAsync(queue, 0, 4, s));
+    const bool sample = samples != nullptr;
+    if (bvh->morton_bits == 63) return dispatch_learn<80>(a, sample, learned, stats != nullptr, s);
+    return dispatch_learn<40>(a, sample, learned, stats != nullptr, s);
 }
 
 template <bool DIS, bool SHADOW, bool AILA, bool STATS, int STACK>

@@ -24,7 +24,10 @@ SYMBOLS = [
     "rta_lbvh_reserve", "rta_lbvh_build", "rta_lbvh_get", "rta_lbvh_status", "rta_lbvh_to_2f4",
     "rta_trace", "rta_setup_shirley_rays", "rta_reset_intersections", "rta_frame_create",
     "rta_frame_destroy", "rta_frame_get", "rta_diffuse_bounce", "rta_frame_run",
-    "rta_frame_status", "rta_diffuse_bounce_noalloc",
+    "rta_frame_status", "rta_diffuse_bounce_noalloc", "rta_order_create", "rta_order_destroy",
+    "rta_order_param_count", "rta_order_get_params", "rta_order_set_params", "rta_order_sample",
+    "rta_order_sample_count", "rta_order_clear_samples", "rta_order_samples", "rta_order_gradient",
+    "rta_order_train", "rta_trace_learned",
 ]
 BOUNCE_NOALLOC_MAX_RAYS = 1 << 24
 
@@ -79,6 +82,18 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_diffuse_bounce.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, u32, f32, vp]
     L.rta_frame_run.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, vp, u32, u32, f32, vp]
     L.rta_frame_status.argtypes = [vp, vp, P(u32)]
+    L.rta_order_create.argtypes = [P(vp), u32, u32]
+    L.rta_order_destroy.argtypes = [vp]
+    L.rta_order_param_count.restype = u32
+    L.rta_order_get_params.argtypes = [vp, vp]
+    L.rta_order_set_params.argtypes = [vp, vp]
+    L.rta_order_sample.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, vp, vp, vp]
+    L.rta_order_sample_count.argtypes = [vp, P(u32)]
+    L.rta_order_clear_samples.argtypes = [vp]
+    L.rta_order_samples.argtypes = [vp, P(vp)]
+    L.rta_order_gradient.argtypes = [vp, u32, u32, vp, vp]
+    L.rta_order_train.argtypes = [vp, u32, u32, f32, vp, vp]
+    L.rta_trace_learned.argtypes = [P(LbvhView), vp, vp, vp, vp, u32, vp, vp, vp, vp]
     L.rta_diffuse_bounce_noalloc.argtypes = [P(LbvhView), vp, vp, vp, u32, u32, f32, vp, vp, vp, vp,
                                              vp, vp]
     for name in SYMBOLS:
@@ -86,7 +101,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
             continue
         fn = getattr(L, name)
         if fn.restype is None or fn.restype is C.c_int:
-            if name not in ("rta_last_error", "rta_lbvh_max_triangles"):
+            if name not in ("rta_last_error", "rta_lbvh_max_triangles", "rta_order_param_count"):
                 fn.restype = C.c_int
     if path == LIB_PATH:
         _lib = L

@@ -1,0 +1,118 @@
+"""The learned child order: the recording traversal is the plain one, samples
+are labelled by the final hit, the tensor-core gradient equals the CPU
+restatement, training lowers the loss, and the learned order keeps every
+closest hit (t bit for bit; a different triangle only at an exact tie)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from oracle import oracle as O  # noqa: E402
+from rta_gb300 import learned as LR  # noqa: E402
+from rta_gb300 import plugin as P  # noqa: E402
+from rta_gb300 import scenes as S  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def terrain_case():
+    tris = S.terrain(256, 128, seed=3)
+    ctor = P.lbvh_constructor(morton_bits=30)
+    bvh = ctor.build(P.cuda_ftl(tris))
+    bvh._ctor = ctor
+    cam = S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), w=640, h=360)
+    g = P.cam_ray_generator_shirley(cam.w, cam.h)
+    g.setup(cam.pos, cam.dir, cam.up, cam.fovy)
+    g.generate_rays()
+    return tris, bvh, g
+
+
+@pytest.fixture(scope="module")
+def cluster_case():
+    tris = S.clusters(32, 2048, seed=4)
+    ctor = P.lbvh_constructor(morton_bits=63)
+    bvh = ctor.build(P.cuda_ftl(tris))
+    bvh._ctor = ctor
+    o, d, m = S.incoherent_rays(200_000, seed=4)
+    dev = torch.device("cuda")
+    return tris, bvh, (torch.from_numpy(o).to(dev), torch.from_numpy(d).to(dev), torch.from_numpy(m).to(dev))
+
+
+def hits_np(h):
+    return h.cpu().numpy().view(O.HIT_DTYPE)
+
+
+def test_recording_trace_is_the_plain_trace(terrain_case):
+    _, bvh, g = terrain_case
+    model = LR.OrderModel(max_samples=1 << 20, seed=1)
+    rec = model.sample(bvh, g.gpu_origin, g.gpu_direction, g.gpu_maxt)
+    plain = LR.plain_trace(bvh, g.gpu_origin, g.gpu_direction, g.gpu_maxt)
+    torch.cuda.synchronize()
+    assert np.array_equal(rec.cpu().numpy().view(np.uint32), plain.cpu().numpy().view(np.uint32))
+    assert model.sample_count() > 0
+
+
+def test_samples_are_labelled_by_the_final_hit(terrain_case):
+    _, bvh, g = terrain_case
+    model = LR.OrderModel(max_samples=1 << 20, seed=1)
+    hits = hits_np(model.sample(bvh, g.gpu_origin, g.gpu_direction, g.gpu_maxt))
+    smp = model.samples().view(O.SAMPLE_DTYPE)
+    assert smp.shape[0] == model.sample_count()
+    ref = hits["ref"][smp["ray"]]
+    hit = hits["t"][smp["ray"]] != np.float32(S.FLT_MAX)
+    in_l = hit & (ref - smp["lfirst"] < smp["lsize"])
+    in_r = hit & ~in_l & (ref - smp["rfirst"] < smp["rsize"])
+    np.testing.assert_array_equal(smp["weight"], (in_l | in_r).astype(np.float32))
+    np.testing.assert_array_equal(smp["label"], in_l.astype(np.float32))
+    # the two children's ranges are disjoint and adjacent (Karras split)
+    lo = np.minimum(smp["lfirst"], smp["rfirst"])
+    assert np.all(smp["lfirst"] + smp["lsize"] == smp["rfirst"])
+    assert lo.size > 0
+
+
+def test_gradient_matches_cpu_restatement(terrain_case):
+    _, bvh, g = terrain_case
+    model = LR.OrderModel(max_samples=1 << 20, seed=7)
+    model.sample(bvh, g.gpu_origin, g.gpu_direction, g.gpu_maxt)
+    n = min(8192, model.sample_count())
+    grad, loss = model.gradient(0, n)
+    smp = model.samples(n).view(O.SAMPLE_DTYPE)
+    x = O.bf16_bits_to_f32(smp["x"].reshape(n, 16))
+    ref, ref_loss = O.mlp_gradient(model.params(), x, smp["label"], smp["weight"], 1.0 / n)
+    scale = np.abs(ref).max()
+    assert np.abs(grad - ref).max() <= 2e-3 * scale, np.abs(grad - ref).max() / scale
+    assert abs(loss - ref_loss / n) <= 1e-3 * abs(ref_loss / n)
+
+
+def test_training_lowers_the_loss(terrain_case):
+    _, bvh, g = terrain_case
+    model = LR.OrderModel(max_samples=1 << 21, seed=3)
+    model.sample(bvh, g.gpu_origin, g.gpu_direction, g.gpu_maxt)
+    n = model.sample_count()
+    _, before = model.gradient(0, n)
+    after = model.train(epochs=4, batch=1 << 14, lr=3e-3)
+    _, now = model.gradient(0, n)
+    assert now < before
+    assert np.isfinite(after)
+
+
+@pytest.mark.parametrize("case", ["terrain", "clusters"])
+def test_learned_order_keeps_closest_hits(case, terrain_case, cluster_case):
+    if case == "terrain":
+        _, bvh, g = terrain_case
+        o, d, m = g.gpu_origin, g.gpu_direction, g.gpu_maxt
+    else:
+        _, bvh, (o, d, m) = cluster_case
+    model = LR.OrderModel(max_samples=1 << 21, seed=5)
+    model.sample(bvh, o, d, m)
+    model.train(epochs=3, batch=1 << 14, lr=3e-3)
+    got, st = model.trace(bvh, o, d, m, stats=True)
+    want, sp = LR.plain_trace(bvh, o, d, m, stats=True)
+    torch.cuda.synchronize()
+    a, b = hits_np(got), hits_np(want)
+    np.testing.assert_array_equal(a["t"].view(np.uint32), b["t"].view(np.uint32))
+    hit = b["t"] != np.float32(S.FLT_MAX)
+    ties = hit & (a["ref"] != b["ref"])
+    assert ties.mean() < 1e-3   # only exact-t ties may report another triangle
+    assert bvh.status() & 0x3F & ~0xC == 0
