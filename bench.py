@@ -47,6 +47,10 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--cpu-sample-rays", type=int, default=262144)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-learned", action="store_true",
+                   help="skip the learned-child-order training and evaluation")
+    p.add_argument("--learned-samples", type=int, default=1 << 24,
+                   help="training decisions recorded over both scene families")
     return p.parse_args()
 
 
@@ -205,6 +209,141 @@ def run_reference(args):
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- #
+# learned child order: train on seeds 0-3, evaluate on seed 4                 #
+# --------------------------------------------------------------------------- #
+
+def _frame_rays(lib, bvh, cam, seed, dev):
+    """Primary rays of `cam` plus one diffuse bounce per hit, on the device."""
+    import torch
+    from rta_gb300 import lib as L
+    from rta_gb300 import plugin as P
+    g = P.cam_ray_generator_shirley(cam.w, cam.h)
+    g.setup(cam.pos, cam.dir, cam.up, cam.fovy)
+    g.generate_rays()
+    n = cam.w * cam.h
+    hits = torch.empty(4 * n, dtype=torch.float32, device=dev)
+    fh = C.c_void_p()
+    L.check(lib.rta_frame_create(C.byref(fh), n), "rta_frame_create")
+    f = L.FrameView()
+    L.check(lib.rta_frame_get(fh, C.byref(f)), "rta_frame_get")
+    L.check(lib.rta_frame_run(fh, C.byref(bvh.view), P._ptr(g.gpu_origin), P._ptr(g.gpu_direction),
+                              P._ptr(g.gpu_maxt), n, P._ptr(hits), L.TRACE_CIS, seed, np.float32(1e-4),
+                              P._stream()), "rta_frame_run")
+    torch.cuda.synchronize()
+    nb = int(P.device_view(f.count, 1, "<u4").cpu().numpy().view(np.uint32)[0])
+    o = torch.cat([g.gpu_origin, P.device_view(f.orig, 3 * nb).clone()])
+    d = torch.cat([g.gpu_direction, P.device_view(f.dir, 3 * nb).clone()])
+    m = torch.cat([g.gpu_maxt, P.device_view(f.maxt, nb).clone()])
+    L.check(lib.rta_frame_destroy(fh), "rta_frame_destroy")
+    return o, d, m
+
+
+def _incoherent(n, seed, dev):
+    import torch
+    from rta_gb300 import scenes as S
+    o, d, m = S.incoherent_rays(n, seed=seed)
+    return (torch.from_numpy(o).to(dev), torch.from_numpy(d).to(dev), torch.from_numpy(m).to(dev))
+
+
+def learned_eval(args, dev):
+    """Configuration 4: the child-order network, trained per scene family on
+    decisions recorded by the plain traversal on seeds 0-3 (half of
+    --learned-samples per family), evaluated on the seed-4 scene of each
+    family with about 8M rays (primary + bounce frame for terrains, 8,388,608
+    incoherent rays for cluster soups)."""
+    import torch
+    from rta_gb300 import learned as LR
+    from rta_gb300 import lib as L
+    from rta_gb300 import plugin as P
+    from rta_gb300 import scenes as S
+    lib = L.load()
+    out = {}
+    per_family = args.learned_samples // 2
+    for fam in ("terrain", "clusters"):
+        bits = 30 if fam == "terrain" else 63
+        make = (lambda sd: S.terrain(1024, 512, seed=sd)) if fam == "terrain" else (lambda sd: S.clusters(seed=sd))
+        model = LR.OrderModel(max_samples=per_family, seed=11)
+        ctor = P.lbvh_constructor(morton_bits=bits, keep_triangles=False)
+        t0 = time.perf_counter()
+        for sd in range(4):
+            bvh = ctor.build(P.cuda_ftl(make(sd)))
+            if fam == "terrain":
+                o, d, m = _frame_rays(lib, bvh, S.terrain_camera(), sd, dev)
+            else:
+                o, d, m = _incoherent(1 << 22, sd, dev)
+            # each seed fills a quarter of the sample store: rays in a seeded
+            # random order, recorded in chunks until the quarter is full
+            perm = torch.from_numpy(np.random.default_rng(sd).permutation(m.numel())).to(dev)
+            target = per_family * (sd + 1) // 4
+            for c0 in range(0, m.numel(), 1 << 18):
+                if model.sample_count() >= target:
+                    break
+                idx = perm[c0:c0 + (1 << 18)]
+                ro = o.view(-1, 3)[idx].contiguous()
+                rd = d.view(-1, 3)[idx].contiguous()
+                model.sample(bvh, ro, rd, m[idx].contiguous())
+        samples = model.sample_count()
+        loss0 = model.gradient(0, min(samples, 1 << 20))[1]
+        loss = model.train(epochs=4, batch=1 << 16, lr=2e-3)
+        train_s = time.perf_counter() - t0
+        bvh = ctor.build(P.cuda_ftl(make(4)))
+        if fam == "terrain":
+            o, d, m = _frame_rays(lib, bvh, S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), w=3200, h=1800), 4, dev)
+        else:
+            o, d, m = _incoherent(1 << 23, 4, dev)
+        nr = int(m.numel())
+        hp, sp = LR.plain_trace(bvh, o, d, m, stats=True)
+        hl, sl = model.trace(bvh, o, d, m, stats=True)
+        _, si = LR.ideal_trace(bvh, o, d, m, hp, stats=True)
+        sin = si.view(-1, 2).to(torch.float64).mean(0).cpu().numpy()
+        a = hp.cpu().numpy().view(np.uint32).reshape(-1, 4)
+        b = hl.cpu().numpy().view(np.uint32).reshape(-1, 4)
+        hit = a[:, 0] != np.float32(3.4028235e38).view(np.uint32)
+        same_hit = bool(np.array_equal(hit, b[:, 0] != np.float32(3.4028235e38).view(np.uint32)))
+        t_other = int((a[:, 0] != b[:, 0]).sum())
+        ta, tb = a[hit, 0].view(np.float32).astype(np.float64), b[hit, 0].view(np.float32).astype(np.float64)
+        t_rel = float((np.abs(ta - tb) / np.abs(ta)).max(initial=0.0))
+        ties = int((hit & (a[:, 3] != b[:, 3])).sum())
+        spn = sp.view(-1, 2).to(torch.float64).mean(0).cpu().numpy()
+        sln = sl.view(-1, 2).to(torch.float64).mean(0).cpu().numpy()
+
+        def timed(fn, k=10):
+            fn()
+            ts = []
+            for _ in range(k):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                fn()
+                e1.record()
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            return statistics.median(ts)
+
+        hbuf = torch.empty(4 * nr, dtype=torch.float32, device=dev)
+        tp = timed(lambda: L.check(lib.rta_trace(C.byref(bvh.view), P._ptr(o), P._ptr(d), P._ptr(m), nr, None,
+                                                 P._ptr(hbuf), L.TRACE_CIS, None, P._stream()), "trace"))
+        tl = timed(lambda: L.check(lib.rta_trace_learned(C.byref(bvh.view), model.handle, P._ptr(o), P._ptr(d),
+                                                         P._ptr(m), nr, None, P._ptr(hbuf), None, P._stream()),
+                                   "trace_learned"))
+        work_p, work_l = float(spn.sum()), float(sln.sum())
+        out[fam] = {
+            "train_samples": samples, "train_loss_before": loss0, "train_loss_after": loss,
+            "train_s": train_s, "eval_rays": nr,
+            "plain": {"nodes_per_ray": float(spn[0]), "tris_per_ray": float(spn[1]), "ms": tp,
+                      "mrays_s": nr / (tp * 1e-3) / 1e6},
+            "learned": {"nodes_per_ray": float(sln[0]), "tris_per_ray": float(sln[1]), "ms": tl,
+                        "mrays_s": nr / (tl * 1e-3) / 1e6},
+            "ideal_order": {"nodes_per_ray": float(sin[0]), "tris_per_ray": float(sin[1]),
+                            "work_reduction": 1.0 - float(sin.sum()) / work_p},
+            "work_reduction": 1.0 - work_l / work_p,
+            "same_rays_hit": same_hit, "rays_t_not_bit_identical": t_other, "t_max_rel_diff": t_rel,
+            "rays_other_triangle": ties,
+            "kept": work_l < work_p,
+        }
+    return out
 
 
 # --------------------------------------------------------------------------- #
@@ -384,6 +523,10 @@ def run_gb300(args):
                "sample": f"{cpu_r['rays']} primary rays evenly strided over the 1920x1080 frame through "
                          f"the spatial-median bbvh of the same terrain (build {cpu_r['build_s']:.2f} s, untimed)"}
 
+    learned = None
+    if not args.no_learned:
+        learned = learned_eval(args, dev)
+
     bmean = statistics.mean(build_ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -412,6 +555,7 @@ def run_gb300(args):
                   "inner_visits_per_bounce_ray": int(stbs[0]) / max(nbounce, 1),
                   "tri_tests_per_primary_ray": int(stp[1]) / nrays,
                   "tri_tests_per_bounce_ray": int(stbs[1]) / max(nbounce, 1)},
+        "learned_order": learned,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -87,6 +87,12 @@ int rta_lbvh_destroy(rta_lbvh_ctx *ctx);
  * n triangles; build() calls it when n grows, as buildCUDA does (lbvh.h:157-162). */
 int rta_lbvh_reserve(rta_lbvh_ctx *ctx, uint32_t n, int morton_bits);
 
+/* Radix digit width of the build's key sort: 8 (default), 10 or 11 bits per
+ * pass.  The sorted order is the same for every width (a stable LSD sort);
+ * wider digits take fewer passes.  The reference sorts with thrust
+ * (sortMortonCodes, lbvh-kernels.cu:537-555), which picks its own width. */
+int rta_lbvh_set_digit_bits(rta_lbvh_ctx *ctx, int digit_bits);
+
 /* lbvh_constructor::buildCUDA (lbvh.h:153-211): initTriangles,
  * calculateVoxelBounds, calculateMortonCodes2, sortMortonCodes,
  * buildTreeKarras, buildBoundingBoxesKarras2, invert_triangle_permutation_cuda
@@ -234,14 +240,26 @@ int rta_order_gradient(rta_order_model *model, uint32_t first, uint32_t count, f
 int rta_order_train(rta_order_model *model, uint32_t epochs, uint32_t batch, float lr,
                     float *last_loss, rta_stream_t stream);
 
-/* Child-is closest-hit trace whose two-child order comes from the network.
- * Every child hit closer than the current t is still visited, so each ray's
- * closest hit is the plain order's, except that of two triangles hit at
- * exactly the same t another one may be found first.  stats as in rta_trace
- * (nullable). */
+/* Child-is closest-hit trace whose two-child order comes from the network
+ * where both children are hit and their entry-exit intervals overlap (the
+ * plain nearer-first order elsewhere).  Every child whose rounded entry
+ * distance is below the current t is still visited, so each ray hits iff it
+ * hits in the plain order, and t agrees up to a few ulps: a triangle's
+ * rounded t can lie just below its box's rounded entry, and of two hits that
+ * close the order decides which survives.  Of two triangles at exactly the
+ * same t another one may be reported.  stats as in rta_trace (nullable). */
 int rta_trace_learned(const rta_lbvh *bvh, const rta_order_model *model, const float *orig,
                       const float *dir, const float *maxt, uint32_t nrays, const uint32_t *d_nrays,
                       void *hits, uint32_t *stats, rta_stream_t stream);
+
+/* The ideal child order, as a bound on what any learned order can gain: the
+ * trace of rta_trace_learned with each decision taken by known_hits (the
+ * ray's closest hit from an earlier trace, 16-byte records as rta_trace
+ * writes them): the child whose Morton range holds the hit triangle first.
+ * No counterpart in the reference. */
+int rta_trace_ideal_order(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt,
+                          uint32_t nrays, const void *known_hits, void *hits, uint32_t *stats,
+                          rta_stream_t stream);
 
 #ifdef __cplusplus
 }

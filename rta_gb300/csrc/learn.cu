@@ -4,7 +4,8 @@
 // records one per node where both children are hit and not culled); the
 // label says which child's subtree holds the ray's final closest hit.  The
 // network (mlp.cuh) is trained with binary cross-entropy and Adam:
-//   k_label     label + weight of each sample from the final hits
+//   k_label     label + weight of each sample from the final hits (weight =
+//               bit length of the other child's triangle count)
 //   k_mlp_grad  forward and backward of 32-row tiles per warp, every product
 //               on mma.sync bf16 with fp32 accumulation; weight gradients
 //               accumulate in registers across tiles, then per block in shared
@@ -40,10 +41,13 @@ __global__ void k_label(Sample *__restrict__ s, const uint32_t *__restrict__ d_c
     for (uint32_t i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         Sample &x = s[i];
         const HitRec h = hits[x.ray];
+        // the weight is the size class (bit length of the triangle count) of
+        // the subtree a wrong first choice would enter: a mistake costs about
+        // the depth of that subtree
         float label = 0.f, weight = 0.f;
         if (h.t != FLT_MAX) {
-            if (h.ref - x.lfirst < x.lsize) { label = 1.f; weight = 1.f; }
-            else if (h.ref - x.rfirst < x.rsize) { label = 0.f; weight = 1.f; }
+            if (h.ref - x.lfirst < x.lsize) { label = 1.f; weight = (float)(32 - __clz(x.rsize)); }
+            else if (h.ref - x.rfirst < x.rsize) { label = 0.f; weight = (float)(32 - __clz(x.lsize)); }
         }
         x.label = label;
         x.weight = weight;
@@ -298,7 +302,7 @@ __global__ void k_adam(float *__restrict__ p, float *__restrict__ m, float *__re
 int trace_learn_impl(const rta_lbvh *bvh, const MlpWeights *w, const float *orig, const float *dir,
                      const float *maxt, uint32_t nrays, const uint32_t *d_nrays, void *hits,
                      uint32_t *stats, Sample *samples, uint32_t *sample_count, uint32_t sample_cap,
-                     uint32_t *queue, bool learned, cudaStream_t s);
+                     uint32_t *queue, bool learned, cudaStream_t s, const void *hint = nullptr);
 
 } // namespace rta
 
@@ -311,6 +315,7 @@ struct rta_order_model {
     float *params = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *loss = nullptr;
     MlpWeights *weights = nullptr;
     int step = 0;
+    uint32_t seed = 0;
 };
 
 static uint32_t host_hash(uint32_t x)
@@ -332,6 +337,7 @@ int rta_order_create(rta_order_model **out, uint32_t max_samples, uint32_t seed)
     if (!out) return RTA_ERR_INVALID;
     rta_order_model *c = new rta_order_model();
     c->cap = max_samples;
+    c->seed = seed;
     cudaError_t e = cudaSuccess;
     if (max_samples) e = cudaMalloc(&c->samples, (size_t)max_samples * sizeof(Sample));
     if (e == cudaSuccess) e = cudaMalloc(&c->counters, 16);
@@ -464,6 +470,9 @@ int rta_order_gradient(rta_order_model *c, uint32_t first, uint32_t count, float
 }
 
 // Adam over the held samples: `epochs` passes of minibatches of `batch` rows.
+// The samples are held in the order the traversal recorded them (ray by ray,
+// scene by scene), so each epoch visits the minibatches in its own shuffled
+// order (Fisher-Yates over the batch indices with the model's hash).
 int rta_order_train(rta_order_model *c, uint32_t epochs, uint32_t batch, float lr, float *last_loss,
                     rta_stream_t stream)
 {
@@ -480,9 +489,21 @@ int rta_order_train(rta_order_model *c, uint32_t epochs, uint32_t batch, float l
         attr = true;
     }
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const uint32_t nbatch = (uint32_t)(((uint64_t)n + batch - 1) / batch);
+    std::vector<uint32_t> order(nbatch);
     for (uint32_t e = 0; e < epochs; ++e) {
+        for (uint32_t i = 0; i < nbatch; ++i) order[i] = i;
+        uint32_t h = host_hash(c->seed ^ host_hash((uint32_t)c->step + e));
+        for (uint32_t i = nbatch; i > 1; --i) {
+            h = host_hash(h + i);
+            const uint32_t j = h % i;
+            const uint32_t t = order[i - 1];
+            order[i - 1] = order[j];
+            order[j] = t;
+        }
         RTA_CUDA_TRY(cudaMemsetAsync(c->loss, 0, 4, s));
-        for (uint32_t first = 0; first < n; first += batch) {
+        for (uint32_t bi = 0; bi < nbatch; ++bi) {
+            const uint32_t first = order[bi] * batch;
             const uint32_t cnt = n - first < batch ? n - first : batch;
             const uint32_t tiles = (cnt + 31) / 32;
             uint32_t blocks = (tiles + kGradWarps - 1) / kGradWarps;
@@ -502,6 +523,15 @@ int rta_order_train(rta_order_model *c, uint32_t epochs, uint32_t batch, float l
         *last_loss = l / (float)n;
     }
     return RTA_OK;
+}
+
+int rta_trace_ideal_order(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt,
+                          uint32_t nrays, const void *known_hits, void *hits, uint32_t *stats,
+                          rta_stream_t stream)
+{
+    if (!bvh || !orig || !dir || !maxt || !known_hits || !hits || nrays == 0) return RTA_ERR_INVALID;
+    return trace_learn_impl(bvh, nullptr, orig, dir, maxt, nrays, nullptr, hits, stats, nullptr, nullptr, 0,
+                            bvh->status + 4, false, (cudaStream_t)stream, known_hits);
 }
 
 int rta_trace_learned(const rta_lbvh *bvh, const rta_order_model *c, const float *orig, const float *dir,

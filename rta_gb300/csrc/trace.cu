@@ -178,6 +178,12 @@ constexpr int kTraceThreads = 128;
 #define RTA_FETCH_IDLE 12
 #endif
 constexpr int kFetchIdle = RTA_FETCH_IDLE;
+// LEARNED: a network pass runs once this many lanes of a warp wait for a
+// decision (or every active lane does)
+#ifndef RTA_PARK_MIN
+#define RTA_PARK_MIN 16
+#endif
+constexpr int kParkMin = RTA_PARK_MIN;
 
 struct Best {
     float t, beta, gamma;
@@ -431,11 +437,16 @@ struct LearnArgs {
     Sample *samples;
     uint32_t *sample_count;
     uint32_t sample_cap;
+    const HitRec *hint;   // HINT: each ray's known closest hit
 };
 
 __device__ __forceinline__ float clampf4(float v) { return fminf(fmaxf(v, -4.0f), 4.0f); }
 
-template <bool SAMPLE, bool LEARNED, bool STATS, int STACK>
+// HINT replaces the network by the ideal decision: the child whose Morton
+// range holds the ray's known closest hit goes first (the plain order where
+// the ray misses).  No predictor can do better than this order, so it bounds
+// what a learned order may gain.
+template <bool SAMPLE, bool LEARNED, bool STATS, int STACK, bool HINT = false>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
 {
     const TraceArgs &A = L.t;
@@ -460,6 +471,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
     Ray R;
     Best best;
     bool overflow = false, capped = false, bad = false;
+    uint32_t hint_ref = 0xffffffffu;   // HINT: Morton position of the known hit
+    bool parked = false;        // LEARNED: waiting for the warp's next network pass
+    uint32_t pq_l = 0, pq_r = 0;   // child links of the parked decision
+    uint32_t px[kMlpIn / 2];    // its features, packed bf16 pairs
 
     for (;;) {
         const uint32_t idle = __ballot_sync(0xffffffffu, !active);
@@ -479,6 +494,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
                         d[k] = A.dir[3 * (size_t)r + k];
                     }
                     make_ray(R, o, d, A.maxt[r]);
+                    if (HINT) {
+                        const HitRec h = L.hint[r];
+                        hint_ref = h.t != FLT_MAX ? h.ref : 0xffffffffu;
+                    }
                     best.t = FLT_MAX;
                     best.beta = best.gamma = 0.f;
                     best.ref = 0;
@@ -497,7 +516,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
         bool done = false, at_inner = false, need = false, hl = false, hr = false;
         NodeRec nd;
         float tnl = FLT_MAX, tfl = FLT_MAX, tnr = FLT_MAX, tfr = FLT_MAX;
-        if (active) {
+        const bool stepping = active && !parked;   // a parked lane waits this step out
+        if (stepping) {
             if (++steps > kMaxSteps) {
                 capped = true;
                 done = true;
@@ -513,14 +533,23 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
                     hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, tnr, tfr);
                     if (tnl >= best.t || tnl > R.tmax) hl = false;
                     if (tnr >= best.t || tnr > R.tmax) hr = false;
-                    need = hl && hr;
+                    // only overlapping entry-exit intervals make the order
+                    // matter: when the nearer child's interval ends before
+                    // the farther one begins, nearer-first is never worse
+                    need = hl && hr && (tnl <= tnr ? tnr < tfl : tnl < tfr);
                 }
             }
         }
         bool left_first = tnl <= tnr;
+        if (HINT && need && hint_ref != 0xffffffffu) {
+            const uint32_t lfirst = is_leaf(nd.q3.x) ? leaf_first(nd.q3.x) : nd.q3.x - nd.q3.z + 1u;
+            const uint32_t rfirst = is_leaf(nd.q3.y) ? leaf_first(nd.q3.y) : nd.q3.y;
+            if (hint_ref - lfirst < nd.q3.z) left_first = true;
+            else if (hint_ref - rfirst < nd.q3.w) left_first = false;
+        }
         if (SAMPLE || LEARNED) {
-            float x[kMlpIn];
             if (need) {
+                float x[kMlpIn];
                 const float base = fminf(tnl, tnr), span = fmaxf(tfl, tfr) - base;
                 const float inv = span > 0.0f ? 1.0f / span : 0.0f;
                 x[0] = clampf4(R.d[0]);
@@ -538,9 +567,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
                 x[12] = (is_leaf(nd.q3.x) ? 1.0f : 0.0f) - (is_leaf(nd.q3.y) ? 1.0f : 0.0f);
                 x[13] = tnl <= tnr ? 1.0f : -1.0f;
                 x[14] = x[15] = 0.0f;
-            } else {
 #pragma unroll
-                for (int k = 0; k < kMlpIn; ++k) x[k] = 0.0f;
+                for (int k = 0; k < kMlpIn / 2; ++k) px[k] = pack_bf16(x[k * 2], x[k * 2 + 1]);
             }
             if (SAMPLE) {
                 const uint32_t m = __ballot_sync(0xffffffffu, need);
@@ -553,7 +581,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
                     if (need && idx < L.sample_cap) {
                         Sample smp;
 #pragma unroll
-                        for (int k = 0; k < kMlpIn; ++k) smp.x[k] = __float2bfloat16_rn(x[k]);
+                        for (int k = 0; k < kMlpIn / 2; ++k)
+                            *reinterpret_cast<uint32_t *>(&smp.x[2 * k]) = px[k];
                         smp.ray = r;
                         smp.lsize = nd.q3.z;
                         smp.rsize = nd.q3.w;
@@ -567,20 +596,42 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
                 }
             }
             if (LEARNED) {
-                if (__any_sync(0xffffffffu, need)) {
+                // a deciding lane parks with its features and both child links
+                // until enough lanes of the warp (or all its active ones) wait,
+                // then one tensor-core pass decides for all of them
+                if (need) {
+                    parked = true;
+                    pq_l = nd.q3.x;
+                    pq_r = nd.q3.y;
+                }
+                const uint32_t pm = __ballot_sync(0xffffffffu, parked);
+                if (pm && (__popc(pm) >= kParkMin || pm == __ballot_sync(0xffffffffu, active))) {
 #pragma unroll
-                    for (int k = 0; k < kMlpIn; k += 2)
-                        *reinterpret_cast<uint32_t *>(&xs[warp][lane][k]) = pack_bf16(x[k], x[k + 1]);
+                    for (int k = 0; k < kMlpIn / 2; ++k)
+                        *reinterpret_cast<uint32_t *>(&xs[warp][lane][2 * k]) = parked ? px[k] : 0u;
                     __syncwarp();
                     MlpForward F;
                     mlp_forward(sw, xs[warp], F);
                     const float logit = mlp_own_logit(F);
                     __syncwarp();
-                    if (need) left_first = logit > 0.0f;
+                    if (parked) {
+                        parked = false;
+                        if (sp + 1 >= STACK) {
+                            overflow = true;
+                            done = true;
+                        } else {
+                            const bool lf = logit > 0.0f;
+                            const uint32_t far = lf ? pq_r : pq_l;
+                            const uint32_t d1 = depth + 1u < 63u ? depth + 1u : 63u;
+                            stack[++sp] = is_leaf(far) ? far : (far | (d1 << kCountShift));
+                            cur = lf ? pq_l : pq_r;
+                            depth = d1;
+                        }
+                    }
                 }
             }
         }
-        if (active && !done) {
+        if (stepping && !done && !(LEARNED && need)) {
             if (at_inner) {
                 if (hl && hr) {
                     if (sp + 1 >= STACK) {
@@ -637,25 +688,28 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
     if (bad) atomicOr(A.status, RTA_DEV_BAD_LINK);
 }
 
-template <bool SAMPLE, bool LEARNED, bool STATS, int STACK>
+template <bool SAMPLE, bool LEARNED, bool STATS, int STACK, bool HINT = false>
 static int launch_learn(const LearnArgs &a, cudaStream_t s)
 {
     static int blocks = 0;
     if (!blocks) {
         int per_sm = 0, dev = 0, sms = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_learn<SAMPLE, LEARNED, STATS, STACK>,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_learn<SAMPLE, LEARNED, STATS, STACK, HINT>,
                                                       kTraceThreads, 0);
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
     }
-    k_trace_learn<SAMPLE, LEARNED, STATS, STACK><<<blocks, kTraceThreads, 0, s>>>(a);
+    k_trace_learn<SAMPLE, LEARNED, STATS, STACK, HINT><<<blocks, kTraceThreads, 0, s>>>(a);
     return check_launch("k_trace_learn");
 }
 
 template <int STACK>
 static int dispatch_learn(const LearnArgs &a, bool sample, bool learned, bool stats, cudaStream_t s)
 {
+    if (a.hint)
+        return stats ? launch_learn<false, false, true, STACK, true>(a, s)
+                     : launch_learn<false, false, false, STACK, true>(a, s);
     if (sample) return launch_learn<true, false, false, STACK>(a, s);
     if (learned) return stats ? launch_learn<false, true, true, STACK>(a, s) : launch_learn<false, true, false, STACK>(a, s);
     return stats ? launch_learn<false, false, true, STACK>(a, s) : launch_learn<false, false, false, STACK>(a, s);
@@ -664,7 +718,7 @@ static int dispatch_learn(const LearnArgs &a, bool sample, bool learned, bool st
 int trace_learn_impl(const rta_lbvh *bvh, const MlpWeights *w, const float *orig, const float *dir,
                      const float *maxt, uint32_t nrays, const uint32_t *d_nrays, void *hits,
                      uint32_t *stats, Sample *samples, uint32_t *sample_count, uint32_t sample_cap,
-                     uint32_t *queue, bool learned, cudaStream_t s)
+                     uint32_t *queue, bool learned, cudaStream_t s, const void *hint)
 {
     LearnArgs a;
     a.t.nodes = (const NodeRec *)bvh->nodes;
@@ -684,6 +738,7 @@ int trace_learn_impl(const rta_lbvh *bvh, const MlpWeights *w, const float *orig
     a.samples = samples;
     a.sample_count = sample_count;
     a.sample_cap = sample_cap;
+    a.hint = (const HitRec *)hint;
     RTA_CUDA_TRY(cudaMemsetAsync(queue, 0, 4, s));
     const bool sample = samples != nullptr;
     if (bvh->morton_bits == 63) return dispatch_learn<80>(a, sample, learned, stats != nullptr, s);

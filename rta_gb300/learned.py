@@ -131,6 +131,19 @@ def plain_trace(bvh, orig, dirs, maxt, stats: bool = False):
     return (hits, st) if stats else hits
 
 
+def ideal_trace(bvh, orig, dirs, maxt, known_hits, stats: bool = False):
+    """Trace with the ideal child order taken from `known_hits` (the closest
+    hits of an earlier trace): the bound on what a learned order can gain."""
+    lib = L.load()
+    n = int(maxt.numel())
+    hits = torch.empty(4 * n, dtype=torch.float32, device=_dev())
+    L.check(lib.rta_reset_intersections(_ptr(hits), n, 1, _stream()), "reset")
+    st = torch.zeros(2 * n, dtype=torch.int32, device=_dev()) if stats else None
+    L.check(lib.rta_trace_ideal_order(C.byref(bvh.view), _ptr(orig), _ptr(dirs), _ptr(maxt), n, _ptr(known_hits),
+                                      _ptr(hits), _ptr(st), _stream()), "rta_trace_ideal_order")
+    return (hits, st) if stats else hits
+
+
 def work_per_ray(stats: torch.Tensor) -> float:
     """Mean nodes + triangles tested per ray."""
     s = stats.view(-1, 2).to(torch.float64)

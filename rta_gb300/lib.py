@@ -21,13 +21,13 @@ TRACE_CIS, TRACE_DIS, TRACE_SHADOW, TRACE_AILA, TRACE_STATS = 0, 1, 2, 4, 8
 # every symbol include/rta_gb300.h declares
 SYMBOLS = [
     "rta_last_error", "rta_lbvh_max_triangles", "rta_lbvh_create", "rta_lbvh_destroy",
-    "rta_lbvh_reserve", "rta_lbvh_build", "rta_lbvh_get", "rta_lbvh_status", "rta_lbvh_to_2f4",
+    "rta_lbvh_reserve", "rta_lbvh_set_digit_bits", "rta_lbvh_build", "rta_lbvh_get", "rta_lbvh_status", "rta_lbvh_to_2f4",
     "rta_trace", "rta_setup_shirley_rays", "rta_reset_intersections", "rta_frame_create",
     "rta_frame_destroy", "rta_frame_get", "rta_diffuse_bounce", "rta_frame_run",
     "rta_frame_status", "rta_diffuse_bounce_noalloc", "rta_order_create", "rta_order_destroy",
     "rta_order_param_count", "rta_order_get_params", "rta_order_set_params", "rta_order_sample",
     "rta_order_sample_count", "rta_order_clear_samples", "rta_order_samples", "rta_order_gradient",
-    "rta_order_train", "rta_trace_learned",
+    "rta_order_train", "rta_trace_learned", "rta_trace_ideal_order",
 ]
 BOUNCE_NOALLOC_MAX_RAYS = 1 << 24
 
@@ -69,6 +69,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_lbvh_create.argtypes = [P(vp)]
     L.rta_lbvh_destroy.argtypes = [vp]
     L.rta_lbvh_reserve.argtypes = [vp, u32, i32]
+    L.rta_lbvh_set_digit_bits.argtypes = [vp, i32]
     L.rta_lbvh_build.argtypes = [vp, vp, u32, i32, vp, vp]
     L.rta_lbvh_get.argtypes = [vp, P(LbvhView)]
     L.rta_lbvh_status.argtypes = [P(LbvhView), vp, P(u32)]
@@ -94,6 +95,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_order_gradient.argtypes = [vp, u32, u32, vp, vp]
     L.rta_order_train.argtypes = [vp, u32, u32, f32, vp, vp]
     L.rta_trace_learned.argtypes = [P(LbvhView), vp, vp, vp, vp, u32, vp, vp, vp, vp]
+    L.rta_trace_ideal_order.argtypes = [P(LbvhView), vp, vp, vp, u32, vp, vp, vp, vp]
     L.rta_diffuse_bounce_noalloc.argtypes = [P(LbvhView), vp, vp, vp, u32, u32, f32, vp, vp, vp, vp,
                                              vp, vp]
     for name in SYMBOLS:

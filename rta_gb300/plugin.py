@@ -154,11 +154,13 @@ class lbvh_constructor:
     """bbvh-cuda/lbvh.h:49-216.  Owns the device buffers (reused while the
     triangle count does not grow, lbvh.h:157-162)."""
 
-    def __init__(self, morton_bits: int = 30, verbose: bool = False, keep_triangles: bool = True):
+    def __init__(self, morton_bits: int = 30, verbose: bool = False, keep_triangles: bool = True,
+                 digit_bits: int = 8):
         self.lib = L.load()
         h = C.c_void_p()
         L.check(self.lib.rta_lbvh_create(C.byref(h)), "rta_lbvh_create")
         self.handle = h
+        L.check(self.lib.rta_lbvh_set_digit_bits(h, digit_bits), "rta_lbvh_set_digit_bits")
         self.morton_bits = morton_bits
         self.verbose = verbose
         self.keep_triangles = keep_triangles

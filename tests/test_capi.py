@@ -50,6 +50,10 @@ def test_invalid_arguments_are_rejected_without_a_device(lib):
         assert lib.rta_lbvh_build(h, C.c_void_p(16), too_many, 30, None, None) == L.ERR_INVALID
         v = L.LbvhView()
         assert lib.rta_lbvh_get(h, C.byref(v)) == L.ERR_INVALID   # nothing built yet
+        for bad in (0, 7, 9, 12):
+            assert lib.rta_lbvh_set_digit_bits(h, bad) == L.ERR_INVALID
+        for good in (8, 10, 11):
+            assert lib.rta_lbvh_set_digit_bits(h, good) == L.OK
     finally:
         assert lib.rta_lbvh_destroy(h) == L.OK
     assert lib.rta_trace(None, None, None, None, 0, None, None, 0, None, None) == L.ERR_INVALID

@@ -63,7 +63,10 @@ def test_samples_are_labelled_by_the_final_hit(terrain_case):
     hit = hits["t"][smp["ray"]] != np.float32(S.FLT_MAX)
     in_l = hit & (ref - smp["lfirst"] < smp["lsize"])
     in_r = hit & ~in_l & (ref - smp["rfirst"] < smp["rsize"])
-    np.testing.assert_array_equal(smp["weight"], (in_l | in_r).astype(np.float32))
+    # weight: bit length of the other child's triangle count
+    bitlen = lambda v: np.frexp(v.astype(np.float64))[1].astype(np.float32)
+    want_w = np.where(in_l, bitlen(smp["rsize"]), np.where(in_r, bitlen(smp["lsize"]), 0.0))
+    np.testing.assert_array_equal(smp["weight"], want_w.astype(np.float32))
     np.testing.assert_array_equal(smp["label"], in_l.astype(np.float32))
     # the two children's ranges are disjoint and adjacent (Karras split)
     lo = np.minimum(smp["lfirst"], smp["rfirst"])
@@ -111,8 +114,15 @@ def test_learned_order_keeps_closest_hits(case, terrain_case, cluster_case):
     want, sp = LR.plain_trace(bvh, o, d, m, stats=True)
     torch.cuda.synchronize()
     a, b = hits_np(got), hits_np(want)
-    np.testing.assert_array_equal(a["t"].view(np.uint32), b["t"].view(np.uint32))
     hit = b["t"] != np.float32(S.FLT_MAX)
+    # a ray hits under either order, and t agrees to 1e-5 relative: a child is
+    # culled once its rounded entry distance reaches the current t, and a
+    # triangle's rounded t can lie a few ulps below its box's entry, so which
+    # of two hits a few ulps apart survives can depend on the order
+    np.testing.assert_array_equal(hit, a["t"] != np.float32(S.FLT_MAX))
+    rel = np.abs(a["t"][hit].astype(np.float64) - b["t"][hit]) / np.abs(b["t"][hit])
+    assert rel.max(initial=0.0) <= 1e-5
+    assert (a["t"] != b["t"]).mean() < 1e-3
     ties = hit & (a["ref"] != b["ref"])
-    assert ties.mean() < 1e-3   # only exact-t ties may report another triangle
+    assert ties.mean() < 1e-3   # ties and those ulp cases may report another triangle
     assert bvh.status() & 0x3F & ~0xC == 0

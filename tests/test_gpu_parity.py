@@ -101,6 +101,19 @@ def test_build_matches_oracle(scene, bits):
                                   O.permute(tris, lb.ids).view(np.uint32))
 
 
+@pytest.mark.parametrize("digit_bits", [10, 11])
+@pytest.mark.parametrize("bits", [30, 63])
+def test_sort_digit_width_gives_the_same_tree(digit_bits, bits):
+    """The stable LSD sort gives one order whatever its digit width (an odd
+    number of passes leaves the result in the second buffer pair)."""
+    tris = S.clusters(32, 2048, seed=5)
+    lb = O.lbvh_build(tris, bits)
+    ctor = P.lbvh_constructor(morton_bits=bits, digit_bits=digit_bits)
+    bvh = ctor.build(P.cuda_ftl(tris))
+    codes = lb.codes if bits == 63 else lb.codes.astype(np.uint32)
+    assert_build_equals(bvh, codes, lb.ids, lb.nodes)
+
+
 def test_rebuild_reuses_buffers_and_matches():
     """Rebuilding with a second, smaller scene through the same constructor
     (the -R path, rta/main.cpp:389-400) gives that scene's tree."""
