@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-learned", action="store_true",
                    help="skip the learned-child-order training and evaluation")
+    p.add_argument("--no-batch", action="store_true",
+                   help="skip the 512-mesh batched build + trace")
     p.add_argument("--learned-samples", type=int, default=1 << 24,
                    help="training decisions recorded over both scene families")
     return p.parse_args()
@@ -347,6 +349,73 @@ def learned_eval(args, dev):
 
 
 # --------------------------------------------------------------------------- #
+# batched multi-mesh: 512 meshes, one graph launch vs per-mesh launches       #
+# --------------------------------------------------------------------------- #
+
+def batch_eval(args, dev):
+    """Configuration 5: 512 seeded meshes (terrains and cluster soups, 1k-200k
+    triangles, about 25M in all) with 4k-1M rays each (about 50M in all, half
+    primary from a per-mesh camera, half incoherent).  All trees are built
+    and all rays traced by one CUDA graph launch with autotuned parameters;
+    the comparison is the per-mesh path (one rta_lbvh_build + one rta_trace
+    per mesh, launched back to back).  Inputs (2.6 GB of triangles, 1.4 GB of
+    rays) are far larger than L2, so no flush is needed between steps."""
+    import tempfile
+
+    import torch
+    from rta_gb300 import batch as BT
+    from rta_gb300 import scenes as S
+
+    t0 = time.perf_counter()
+    work = BT.make_workload(S.batch_specs(512, seed=0))
+    gen_s = time.perf_counter() - t0
+    b = BT.Batch()
+    b.set_meshes(work.tri_offsets, work.ray_offsets)
+    nr = work.n_rays
+    hits = torch.zeros(4 * nr, dtype=torch.float32, device=dev)
+    cache = os.path.join(tempfile.gettempdir(), "rta_gb300_autotune.json")
+    if os.path.exists(cache):
+        os.remove(cache)   # tune afresh: the timing is part of what is reported
+    t0 = time.perf_counter()
+    chosen, tuned_ms = b.autotune(work.tris, work.orig, work.dirs, work.maxt, hits, cache_path=cache, reps=3)
+    tune_s = time.perf_counter() - t0
+
+    def timed(fn, k):
+        ts = []
+        for _ in range(k):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    steps = max(3, min(args.steps, 10))
+    for _ in range(3):
+        b.run(work.tris, work.orig, work.dirs, work.maxt, hits)
+    graph_ms = timed(lambda: b.run(work.tris, work.orig, work.dirs, work.maxt, hits), steps)
+    torch.cuda.synchronize()
+    batch_hits = hits.clone()
+    build_ms = timed(lambda: b.build(work.tris), steps)
+    trace_ms = timed(lambda: b.trace(work.orig, work.dirs, work.maxt, hits), steps)
+    seq_hits = torch.zeros_like(hits)
+    ctor = BT.sequential(work, seq_hits)   # warm-up (allocates the largest mesh's buffers)
+    seq_ms = timed(lambda: BT.sequential(work, seq_hits, ctor), max(3, steps // 3))
+    torch.cuda.synchronize()
+    same = bool(torch.equal(seq_hits.view(torch.int32), batch_hits.view(torch.int32)))
+    return {
+        "meshes": len(work.tri_offsets) - 1, "triangles": work.n_tris, "rays": nr,
+        "graph_ms": graph_ms, "build_ms": build_ms, "trace_ms": trace_ms,
+        "build_mtri_s": work.n_tris / (build_ms * 1e-3) / 1e6, "trace_mrays_s": nr / (trace_ms * 1e-3) / 1e6,
+        "graph_mrays_s": nr / (graph_ms * 1e-3) / 1e6,
+        "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / graph_ms,
+        "identical_hits_vs_sequential": same, "params": chosen, "autotune_s": tune_s,
+        "autotune_best_ms": tuned_ms, "workload_gen_s": gen_s,
+    }
+
+
+# --------------------------------------------------------------------------- #
 # GB300 arm                                                                   #
 # --------------------------------------------------------------------------- #
 
@@ -526,6 +595,9 @@ def run_gb300(args):
     learned = None
     if not args.no_learned:
         learned = learned_eval(args, dev)
+    batched = None
+    if not args.no_batch:
+        batched = batch_eval(args, dev)
 
     bmean = statistics.mean(build_ms)
     line = {
@@ -556,6 +628,7 @@ def run_gb300(args):
                   "tri_tests_per_primary_ray": int(stp[1]) / nrays,
                   "tri_tests_per_bounce_ray": int(stbs[1]) / max(nbounce, 1)},
         "learned_order": learned,
+        "batched": batched,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

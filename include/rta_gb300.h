@@ -261,6 +261,83 @@ int rta_trace_ideal_order(const rta_lbvh *bvh, const float *orig, const float *d
                           uint32_t nrays, const void *known_hits, void *hits, uint32_t *stats,
                           rta_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* Batched multi-mesh build and trace                                        */
+/* ------------------------------------------------------------------------ */
+/* Many independent meshes, each with its own 30-bit LBVH over its own box and
+ * its own rays, built and traced together: one sort of (mesh id, Morton code)
+ * keys, the Karras trees and refits of all meshes in one launch each, and one
+ * persistent trace launch over all rays in which every lane looks up its
+ * ray's mesh.  Each mesh's tree, index buffer and hits are bit-identical to
+ * rta_lbvh_build + rta_trace of that mesh alone (its triangle ids and hit
+ * refs are local to the mesh).  No counterpart in the reference, which builds
+ * one mesh per lbvh_constructor (lbvh.h:153-211). */
+typedef struct rta_batch rta_batch;
+
+/* Launch parameters of a batch (chosen by rta_batch_autotune or set). */
+typedef struct rta_batch_params {
+    int digit_bits;     /* sort digit width: 8, 10 or 11 */
+    int fetch_idle;     /* a warp fetches rays once this many lanes are idle: 1..32 */
+    int blocks_per_sm;  /* persistent trace blocks per SM, 0 = occupancy maximum */
+    int stack;          /* traversal stack entries: 40 or 64 */
+} rta_batch_params;
+
+int rta_batch_create(rta_batch **out);
+int rta_batch_destroy(rta_batch *b);
+
+/* Declares the meshes and sizes the device buffers.  tri_offsets and
+ * ray_offsets are HOST prefix arrays of meshes + 1 entries: mesh m owns
+ * triangles [tri_offsets[m], tri_offsets[m+1]) of the concatenated input
+ * (1 .. rta_lbvh_max_triangles() of them) and rays [ray_offsets[m],
+ * ray_offsets[m+1]) (possibly none).  At most 2^20 meshes. */
+int rta_batch_set_meshes(rta_batch *b, uint32_t meshes, const uint32_t *tri_offsets,
+                         const uint32_t *ray_offsets);
+
+/* Builds every mesh's LBVH from the concatenated 104-byte records (device). */
+int rta_batch_build(rta_batch *b, const void *tris, rta_stream_t stream);
+
+/* Closest-hit (child-is) trace of every mesh's rays against its own tree:
+ * rays in the rta_trace layout, concatenated in mesh order; hits (16 bytes
+ * per ray, t = FLT_MAX on entry as rta_reset_intersections leaves it) are
+ * written in the same order; stats as in rta_trace (nullable). */
+int rta_batch_trace(rta_batch *b, const float *orig, const float *dir, const float *maxt, void *hits,
+                    uint32_t *stats, rta_stream_t stream);
+
+/* Build + hit reset (as rta_reset_intersections) + trace as one CUDA graph launch.  The graph is captured
+ * on the first call and again whenever the pointers or the parameters
+ * change; the call that captures also launches it. */
+int rta_batch_run(rta_batch *b, const void *tris, const float *orig, const float *dir,
+                  const float *maxt, void *hits, rta_stream_t stream);
+
+/* The tree of one mesh as a one-mesh view (for rta_trace, rta_lbvh_to_2f4
+ * and the parity checks).  Valid until the next set_meshes / destroy. */
+int rta_batch_mesh(const rta_batch *b, uint32_t mesh, rta_lbvh *out);
+
+/* Device flags of the last build / trace (RTA_DEV_*); synchronises stream. */
+int rta_batch_status(const rta_batch *b, rta_stream_t stream, uint32_t *flags);
+
+int rta_batch_get_params(const rta_batch *b, rta_batch_params *p);
+int rta_batch_set_params(rta_batch *b, const rta_batch_params *p);
+
+/* Autotuner: times rta_batch_run (median of reps graph launches) while it
+ * walks the parameters one at a time over their candidate values (digit
+ * width, fetch threshold, blocks per SM, stack), keeps the fastest and sets
+ * it.  With a cache_path (nullable), a cached choice for this device and
+ * workload is used without timing, and a new choice is stored there. */
+int rta_batch_autotune(rta_batch *b, const void *tris, const float *orig, const float *dir,
+                       const float *maxt, void *hits, const char *cache_path, int reps,
+                       rta_stream_t stream, rta_batch_params *chosen, float *best_ms);
+
+/* The autotuner's cache key of b (device name, SM count, mesh count and the
+ * power-of-two classes of the triangle and ray counts). */
+int rta_batch_tune_key(const rta_batch *b, char *buf, uint32_t size);
+
+/* The tuning cache: a JSON object, one entry per line, key -> parameters and
+ * time.  Work without a device.  lookup returns RTA_ERR_INVALID when the
+ * file or the key is absent. */
+int rta_tune_cache_lookup(const char *path, const char *key, rta_batch_params *p);
+int rta_tune_cache_store(const char *path, const char *key, const rta_batch_params *p, float ms);
+
 #ifdef __cplusplus
 }
 #endif

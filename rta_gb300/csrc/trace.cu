@@ -13,6 +13,7 @@
 //   DIS  trace_dis(float4*)  (bbvh-cuda/kernels.cu:486-548)
 // so hits, including which of two equal-t triangles wins, are the reference's.
 #include "common.cuh"
+#include "batch.cuh"
 #include "mlp.cuh"
 
 namespace rta {
@@ -416,6 +417,187 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(TraceArgs A)
     if (overflow) atomicOr(A.status, RTA_DEV_STACK_OVERFLOW);
     if (capped) atomicOr(A.status, RTA_DEV_ITER_LIMIT);
     if (bad) atomicOr(A.status, RTA_DEV_BAD_LINK);
+}
+
+// ------------------------------------------------------------------------- //
+// batched child-is traversal: many meshes, one persistent launch             //
+// ------------------------------------------------------------------------- //
+//
+// The step loop of k_trace<CIS> over the rays of all meshes of a batch.  A
+// lane that takes ray r finds its mesh by a binary search over the rays'
+// prefix offsets and from then on walks that mesh's tree (its own node,
+// triangle and root pointers), so the warps stay full across mesh borders.
+// fetch_idle is a launch parameter here (the autotuner sets it).
+
+template <bool STATS, int STACK>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_batch(BatchTraceArgs A)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const uint32_t nrays = A.nrays;
+
+    bool active = false, exhausted = false;
+    uint32_t r = 0, cur = 0, steps = 0, inner_visits = 0, tri_tests = 0;
+    int sp = -1;
+    uint32_t stack[STACK];
+    Ray R;
+    Best best;
+    const NodeRec *nodes = nullptr;
+    const TriRec *tris = nullptr;
+    uint32_t n_tris = 1, n_inner = 0;
+    bool overflow = false, capped = false, bad = false;
+
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && __popc(idle) >= A.fetch_idle) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(A.queue, (uint32_t)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base >= nrays) {
+                exhausted = true;
+            } else if (!active) {
+                r = base + __popc(idle & lt_mask);
+                if (r < nrays) {
+                    const uint32_t m = find_range(A.ray_off, A.n_meshes, r);
+                    const MeshRec mr = A.meshes[m];
+                    nodes = A.nodes + mr.node_off;
+                    tris = A.tris + mr.tri_off;
+                    n_tris = mr.n_tris;
+                    n_inner = n_tris - 1u;
+                    float o[3], d[3];
+                    o[0] = A.orig[3 * (size_t)r + 0];
+                    o[1] = A.orig[3 * (size_t)r + 1];
+                    o[2] = A.orig[3 * (size_t)r + 2];
+                    d[0] = A.dir[3 * (size_t)r + 0];
+                    d[1] = A.dir[3 * (size_t)r + 1];
+                    d[2] = A.dir[3 * (size_t)r + 2];
+                    make_ray(R, o, d, A.maxt[r]);
+                    best.t = FLT_MAX;
+                    best.beta = best.gamma = 0.f;
+                    best.ref = 0;
+                    sp = -1;
+                    steps = inner_visits = tri_tests = 0;
+                    cur = A.roots[m].link;
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (!active) continue;
+
+        bool done = false;
+        if (++steps > kMaxSteps) {
+            capped = true;
+            done = true;
+        } else if (!is_leaf(cur)) {
+            if (cur >= n_inner) {
+                bad = true;
+                done = true;
+            } else {
+                ++inner_visits;
+                const NodeRec nd = load_node(nodes, cur);
+                float dl = FLT_MAX, dr = FLT_MAX;
+                bool hl = slab_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, dl);
+                bool hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, dr);
+                if (dl >= best.t || dl > R.tmax) hl = false;
+                if (dr >= best.t || dr > R.tmax) hr = false;
+                if (hl && hr) {
+                    if (sp + 1 >= STACK) {
+                        overflow = true;
+                        done = true;
+                    } else if (dl <= dr) {
+                        stack[++sp] = nd.q3.y;
+                        cur = nd.q3.x;
+                    } else {
+                        stack[++sp] = nd.q3.x;
+                        cur = nd.q3.y;
+                    }
+                } else if (hl) {
+                    cur = nd.q3.x;
+                } else if (hr) {
+                    cur = nd.q3.y;
+                } else if (sp < 0) {
+                    done = true;
+                } else {
+                    cur = stack[sp--];
+                }
+            }
+        } else {
+            if (visit_leaf<false>(tris, n_tris, cur, R.o, R.d, R.tmax, best, tri_tests, bad))
+                done = true;
+            else if (sp < 0)
+                done = true;
+            else
+                cur = stack[sp--];
+        }
+        if (done) {
+            if (best.t != FLT_MAX) {
+                reinterpret_cast<float4 *>(A.hits)[r] =
+                    make_float4(best.t, best.beta, best.gamma, __uint_as_float(best.ref));
+            } else {
+                A.hits[r].t = FLT_MAX;
+            }
+            if (STATS) {
+                A.stats[2 * (size_t)r + 0] = inner_visits;
+                A.stats[2 * (size_t)r + 1] = tri_tests;
+            }
+            active = false;
+        }
+    }
+    if (overflow) atomicOr(A.status, RTA_DEV_STACK_OVERFLOW);
+    if (capped) atomicOr(A.status, RTA_DEV_ITER_LIMIT);
+    if (bad) atomicOr(A.status, RTA_DEV_BAD_LINK);
+}
+
+// occupancy limit and SM count, queried once (before any graph capture:
+// prepare_batch_trace() is called outside capture)
+template <bool STATS, int STACK>
+static void batch_grid(int &max_per_sm, int &sms)
+{
+    static int m = 0, n = 0;
+    if (!m) {
+        int dev = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_trace_batch<STATS, STACK>, kTraceThreads, 0);
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (m <= 0) m = 1;
+        if (n <= 0) n = 1;
+    }
+    max_per_sm = m;
+    sms = n;
+}
+
+template <bool STATS, int STACK>
+static int launch_batch(const BatchTraceArgs &a, int blocks_per_sm, cudaStream_t s)
+{
+    int max_per_sm, sms;
+    batch_grid<STATS, STACK>(max_per_sm, sms);
+    const int per_sm = blocks_per_sm > 0 && blocks_per_sm < max_per_sm ? blocks_per_sm : max_per_sm;
+    k_trace_batch<STATS, STACK><<<per_sm * sms, kTraceThreads, 0, s>>>(a);
+    return check_launch("k_trace_batch");
+}
+
+int batch_trace_max_blocks_per_sm(int stack)
+{
+    int m, n;
+    if (stack == 64) batch_grid<false, 64>(m, n);
+    else batch_grid<false, 40>(m, n);
+    batch_grid<true, 40>(m, n);
+    batch_grid<true, 64>(m, n);
+    if (stack == 64) batch_grid<false, 64>(m, n);
+    else batch_grid<false, 40>(m, n);
+    return m;
+}
+
+int launch_batch_trace(const BatchTraceArgs &a, int stack, int blocks_per_sm, cudaStream_t s)
+{
+    if (stack == 64)
+        return a.stats ? launch_batch<true, 64>(a, blocks_per_sm, s) : launch_batch<false, 64>(a, blocks_per_sm, s);
+    return a.stats ? launch_batch<true, 40>(a, blocks_per_sm, s) : launch_batch<false, 40>(a, blocks_per_sm, s);
 }
 
 // ------------------------------------------------------------------------- //

@@ -28,6 +28,9 @@ SYMBOLS = [
     "rta_order_param_count", "rta_order_get_params", "rta_order_set_params", "rta_order_sample",
     "rta_order_sample_count", "rta_order_clear_samples", "rta_order_samples", "rta_order_gradient",
     "rta_order_train", "rta_trace_learned", "rta_trace_ideal_order",
+    "rta_batch_create", "rta_batch_destroy", "rta_batch_set_meshes", "rta_batch_build", "rta_batch_trace",
+    "rta_batch_run", "rta_batch_mesh", "rta_batch_status", "rta_batch_get_params", "rta_batch_set_params",
+    "rta_batch_autotune", "rta_batch_tune_key", "rta_tune_cache_lookup", "rta_tune_cache_store",
 ]
 BOUNCE_NOALLOC_MAX_RAYS = 1 << 24
 
@@ -48,6 +51,15 @@ class FrameView(C.Structure):
     _fields_ = [("orig", C.c_void_p), ("dir", C.c_void_p), ("maxt", C.c_void_p),
                 ("src", C.c_void_p), ("hits", C.c_void_p), ("count", C.c_void_p),
                 ("capacity", C.c_uint32)]
+
+
+class BatchParams(C.Structure):
+    """struct rta_batch_params"""
+    _fields_ = [("digit_bits", C.c_int32), ("fetch_idle", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("stack", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
 
 
 _lib = None
@@ -98,6 +110,20 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_trace_ideal_order.argtypes = [P(LbvhView), vp, vp, vp, u32, vp, vp, vp, vp]
     L.rta_diffuse_bounce_noalloc.argtypes = [P(LbvhView), vp, vp, vp, u32, u32, f32, vp, vp, vp, vp,
                                              vp, vp]
+    L.rta_batch_create.argtypes = [P(vp)]
+    L.rta_batch_destroy.argtypes = [vp]
+    L.rta_batch_set_meshes.argtypes = [vp, u32, vp, vp]
+    L.rta_batch_build.argtypes = [vp, vp, vp]
+    L.rta_batch_trace.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.rta_batch_run.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.rta_batch_mesh.argtypes = [vp, u32, P(LbvhView)]
+    L.rta_batch_status.argtypes = [vp, vp, P(u32)]
+    L.rta_batch_get_params.argtypes = [vp, P(BatchParams)]
+    L.rta_batch_set_params.argtypes = [vp, P(BatchParams)]
+    L.rta_batch_autotune.argtypes = [vp, vp, vp, vp, vp, vp, C.c_char_p, i32, vp, P(BatchParams), P(f32)]
+    L.rta_batch_tune_key.argtypes = [vp, C.c_char_p, u32]
+    L.rta_tune_cache_lookup.argtypes = [C.c_char_p, C.c_char_p, P(BatchParams)]
+    L.rta_tune_cache_store.argtypes = [C.c_char_p, C.c_char_p, P(BatchParams), f32]
     for name in SYMBOLS:
         if not hasattr(L, name):
             continue

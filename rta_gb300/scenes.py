@@ -226,3 +226,83 @@ def incoherent_rays(n: int, extent: float = 12.0, seed: int = 0):
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     maxt = np.full(n, FLT_MAX, np.float32)
     return orig.reshape(-1), d.astype(np.float32).reshape(-1), maxt
+
+
+# --------------------------------------------------------------------------- #
+# batched multi-mesh workload                                                 #
+# --------------------------------------------------------------------------- #
+
+class MeshSpec:
+    """One mesh of a batch: its kind, triangle count, camera and ray split."""
+
+    def __init__(self, kind, n_tris, seed, n_rays, cam, n_primary):
+        self.kind, self.n_tris, self.seed = kind, n_tris, seed
+        self.n_rays, self.cam, self.n_primary = n_rays, cam, n_primary
+
+
+def _lognormal_counts(rng, count, lo, hi, target_total, sigma):
+    """`count` lognormal sizes clipped to [lo, hi] whose sum is close to
+    target_total (the median is found by bisection on the same draws)."""
+    z = rng.normal(size=count)
+    a, b = math.log(lo), math.log(hi)
+    for _ in range(60):
+        mu = 0.5 * (a + b)
+        tot = np.clip(np.exp(mu + sigma * z), lo, hi).astype(np.int64).sum()
+        if tot < target_total:
+            a = mu
+        else:
+            b = mu
+    return np.clip(np.exp(0.5 * (a + b) + sigma * z), lo, hi).astype(np.int64)
+
+
+def batch_specs(meshes: int = 512, seed: int = 0, total_tris: int = 25_000_000,
+                tri_range=(1000, 200_000), total_rays: int = 50_000_000, ray_range=(4096, 1 << 20)):
+    """The batched workload: `meshes` independent meshes, each a terrain
+    (heightfield with fBm height, like the 1M-triangle terrain) or a cluster
+    soup (Gaussian clusters, like the 4M-triangle one), chosen by a coin flip;
+    triangle counts lognormal clipped to tri_range with a sum near total_tris;
+    per-mesh ray counts lognormal clipped to ray_range with a sum near
+    total_rays, half of them primary rays of a per-mesh pinhole camera, the
+    rest incoherent (origins uniform in the mesh box grown by 20 %, directions
+    uniform on the sphere)."""
+    rng = np.random.default_rng(seed + 104729)
+    nt = _lognormal_counts(rng, meshes, tri_range[0], tri_range[1], total_tris, 1.0)
+    nr = _lognormal_counts(rng, meshes, ray_range[0], ray_range[1], total_rays, 1.0)
+    kinds = np.where(rng.uniform(size=meshes) < 0.5, "terrain", "clusters")
+    out = []
+    for m in range(meshes):
+        half = int(nr[m]) // 2
+        h = max(1, int(math.sqrt(half * 9.0 / 16.0)))
+        w = max(1, half // h)
+        if kinds[m] == "terrain":
+            cam = Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), fovy=60.0, w=w, h=h)
+        else:
+            cam = Camera((0.0, 4.0, 30.0), (0.0, 0.0, 0.0), fovy=60.0, w=w, h=h)
+        out.append(MeshSpec(str(kinds[m]), int(nt[m]), seed * 100003 + m, int(nr[m]), cam, w * h))
+    return out
+
+
+def batch_mesh_triangles(spec: MeshSpec) -> np.ndarray:
+    """The triangles of one batch mesh (104-byte records), exactly n_tris."""
+    n = spec.n_tris
+    if spec.kind == "terrain":
+        nz = max(1, int(math.sqrt(n / 4.0)))
+        nx = max(1, -(-n // (2 * nz)))
+        t = terrain(nx, nz, seed=spec.seed)
+    else:
+        k = max(1, min(256, n // 64))
+        t = clusters(k, -(-n // k), seed=spec.seed)
+    return np.ascontiguousarray(t[:n])
+
+
+def batch_incoherent_rays(spec: MeshSpec, tris: np.ndarray):
+    """The incoherent half of a mesh's rays."""
+    n = spec.n_rays - spec.n_primary
+    rng = np.random.default_rng(spec.seed + 7919)
+    p = tris[:, 0:9].reshape(-1, 3)
+    lo, hi = p.min(0), p.max(0)
+    c, e = 0.5 * (lo + hi), 0.6 * (hi - lo)
+    orig = (c + rng.uniform(-1.0, 1.0, size=(n, 3)) * e).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return orig.reshape(-1), d.astype(np.float32).reshape(-1), np.full(n, FLT_MAX, np.float32)
