@@ -51,6 +51,10 @@ def parse():
                    help="skip the learned-child-order training and evaluation")
     p.add_argument("--no-batch", action="store_true",
                    help="skip the 512-mesh batched build + trace")
+    p.add_argument("--no-incoherent", action="store_true",
+                   help="skip the 4M-triangle 63-bit build + 8M incoherent rays")
+    p.add_argument("--section", choices=["incoherent", "learned", "batched"], default=None,
+                   help="run only this workload and print its JSON object (not the bench line)")
     p.add_argument("--learned-samples", type=int, default=1 << 24,
                    help="training decisions recorded over both scene families")
     return p.parse_args()
@@ -349,6 +353,77 @@ def learned_eval(args, dev):
 
 
 # --------------------------------------------------------------------------- #
+# incoherent large scene: 4M clustered triangles, 63-bit codes, 8M rays       #
+# --------------------------------------------------------------------------- #
+
+def incoherent_eval(args, dev):
+    """Configuration 3: 4,194,304 triangles in 256 Gaussian clusters, 63-bit
+    Morton codes (the build's bandwidth case: 1.5 GB of build traffic), and
+    8,388,608 rays with origins uniform in [-12, 12]^3 and directions uniform
+    on the sphere.  Build and trace are timed separately (CUDA events, L2
+    flushed before each step); the per-ray work comes from one stats pass."""
+    import torch
+    from rta_gb300 import lib as L
+    from rta_gb300 import plugin as P
+    from rta_gb300 import scenes as S
+
+    lib = L.load()
+    tris = S.clusters(256, 16384, seed=SEED)
+    n = tris.shape[0]
+    ftl = P.cuda_ftl(tris)
+    ctor = P.lbvh_constructor(morton_bits=63, keep_triangles=False)
+    o, d, m = (torch.from_numpy(x).to(dev) for x in S.incoherent_rays(1 << 23, seed=SEED))
+    nr = int(m.numel())
+    hits = torch.empty(4 * nr, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    sh = P._stream()
+
+    def timed(fn, k):
+        ts = []
+        for _ in range(k):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    def build():
+        L.check(lib.rta_lbvh_build(ctor.handle, P._ptr(ftl.triangle), n, 63, C.c_void_p(0), sh), "build")
+
+    for _ in range(args.warmup):
+        build()
+    k = max(3, min(args.steps, 50))
+    build_ms = timed(build, k)
+    bvh = P.binary_lbvh(ctor, None)
+
+    def trace(mode=L.TRACE_CIS, st=None):
+        L.check(lib.rta_trace(C.byref(bvh.view), P._ptr(o), P._ptr(d), P._ptr(m), nr, C.c_void_p(0), P._ptr(hits),
+                              mode, P._ptr(st), sh), "trace")
+
+    for _ in range(max(1, args.warmup // 2)):
+        trace()
+    trace_ms = timed(trace, max(3, min(args.steps, 20)))
+    st = torch.zeros(2 * nr, dtype=torch.int32, device=dev)
+    trace(L.TRACE_CIS | L.TRACE_STATS, st)
+    w = st.view(-1, 2).to(torch.float64).mean(0).cpu().numpy()
+    torch.cuda.synchronize()
+    hit_frac = float((hits.view(-1, 4)[:, 0] < 3.0e38).to(torch.float64).mean())
+    alg = 504 * n   # build bytes per triangle with 63-bit keys (8 sort passes of 12-byte keys+ids)
+    peak, _ = measured_peaks()
+    return {
+        "triangles": n, "morton_bits": 63, "rays": nr, "hit_fraction": hit_frac,
+        "build_ms": build_ms, "build_mtri_s": n / (build_ms * 1e-3) / 1e6,
+        "build_algorithmic_bytes": alg, "build_gbs": alg / (build_ms * 1e-3) / 1e9,
+        "build_frac_of_peak": alg / (build_ms * 1e-3) / 1e9 / peak,
+        "trace_ms": trace_ms, "trace_mrays_s": nr / (trace_ms * 1e-3) / 1e6,
+        "inner_visits_per_ray": float(w[0]), "tri_tests_per_ray": float(w[1]),
+    }
+
+
+# --------------------------------------------------------------------------- #
 # batched multi-mesh: 512 meshes, one graph launch vs per-mesh launches       #
 # --------------------------------------------------------------------------- #
 
@@ -547,16 +622,17 @@ def run_gb300(args):
     h_maxt.copy_(rg.gpu_maxt)
     h_hits = torch.empty(nrays * 4, dtype=torch.float32, pin_memory=True)
     h_bhits = torch.empty(nrays * 4, dtype=torch.float32, pin_memory=True)
-    d_orig, d_dir, d_maxt = torch.empty_like(rg.gpu_origin), torch.empty_like(rg.gpu_direction), torch.empty_like(rg.gpu_maxt)
     bhits_view = P.device_view(frame.hits, 4 * nrays)
 
+    # The frame is called with the pinned HOST buffers themselves: on GB300
+    # the GPU reads the rays and writes the primary hits over NVLink-C2C
+    # while it traces (pinned memory is device-addressable under unified
+    # addressing), so the transfers overlap the traversal instead of
+    # preceding and following it.  The bounce hits stay in the frame's
+    # device buffer and are copied back after the frame.
     def e2e_step():
-        d_orig.copy_(h_orig, non_blocking=True)
-        d_dir.copy_(h_dir, non_blocking=True)
-        d_maxt.copy_(h_maxt, non_blocking=True)
-        L.check(lib.rta_frame_run(fh, C.byref(bvh.view), P._ptr(d_orig), P._ptr(d_dir), P._ptr(d_maxt),
-                                  nrays, P._ptr(hits), L.TRACE_CIS, SEED, np.float32(1e-4), sh), "frame")
-        h_hits.copy_(hits, non_blocking=True)
+        L.check(lib.rta_frame_run(fh, C.byref(bvh.view), P._ptr(h_orig), P._ptr(h_dir), P._ptr(h_maxt),
+                                  nrays, P._ptr(h_hits), L.TRACE_CIS, SEED, np.float32(1e-4), sh), "frame")
         h_bhits[: 4 * nbounce].copy_(bhits_view[: 4 * nbounce], non_blocking=True)
 
     for _ in range(max(1, args.warmup)):
@@ -572,6 +648,11 @@ def run_gb300(args):
     h2d = (3 + 3 + 1) * 4 * nrays
     d2h = 16 * nrays + 16 * nbounce
     e2e_value = rays_per_step * world / (e2e_ms * 1e-3) / 1e6
+    # the zero-copy frame gives the same hits as the device-resident one
+    torch.cuda.synchronize()
+    ha, hb = h_hits.view(torch.int32).view(-1, 4), hits.cpu().view(torch.int32).view(-1, 4)
+    hit_rows = ha[:, 0] != 0x7F7FFFFF   # t != FLT_MAX (a miss writes only t)
+    e2e_same = bool(torch.equal(ha[:, 0], hb[:, 0]) and torch.equal(ha[hit_rows], hb[hit_rows]))
 
     # ---- roofline of the primary trace kernel ----
     peak, peak_kind = measured_peaks()
@@ -592,6 +673,9 @@ def run_gb300(args):
                "sample": f"{cpu_r['rays']} primary rays evenly strided over the 1920x1080 frame through "
                          f"the spatial-median bbvh of the same terrain (build {cpu_r['build_s']:.2f} s, untimed)"}
 
+    incoherent = None
+    if not args.no_incoherent:
+        incoherent = incoherent_eval(args, dev)
     learned = None
     if not args.no_learned:
         learned = learned_eval(args, dev)
@@ -614,7 +698,9 @@ def run_gb300(args):
                      "peak_source": peak_kind},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_ms},
+                "ms_per_step": e2e_ms, "hits_equal_device_run": e2e_same,
+                "how": "rta_frame_run on pinned host rays and hits (read/written by the kernels over "
+                       "NVLink-C2C), bounce hits copied device-to-host; one call per step"},
         "gpu_launches": 5 * args.steps,
         "clocks": clk.summary(),
         "build": {"ms": bmean, "ms_min": min(build_ms), "mtri_s": n / (bmean * 1e-3) / 1e6,
@@ -627,6 +713,7 @@ def run_gb300(args):
                   "inner_visits_per_bounce_ray": int(stbs[0]) / max(nbounce, 1),
                   "tri_tests_per_primary_ray": int(stp[1]) / nrays,
                   "tri_tests_per_bounce_ray": int(stbs[1]) / max(nbounce, 1)},
+        "incoherent": incoherent,
         "learned_order": learned,
         "batched": batched,
     }
@@ -637,10 +724,21 @@ def run_gb300(args):
         pg.destroy_process_group()
 
 
+def run_section(args):
+    """One workload alone (for profiling and quick checks): prints its object."""
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    fn = {"incoherent": incoherent_eval, "learned": learned_eval, "batched": batch_eval}[args.section]
+    print(json.dumps({args.section: fn(args, dev)}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.section:
+        run_section(args)
     else:
         run_gb300(args)
 

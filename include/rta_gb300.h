@@ -175,7 +175,13 @@ int rta_diffuse_bounce(rta_frame_ctx *ctx, const rta_lbvh *bvh, const float *ori
                        float eps, rta_stream_t stream);
 
 /* Whole frame: reset primary hits, trace primary rays, generate the bounce,
- * reset bounce hits, trace the bounce rays.  No host synchronisation. */
+ * reset bounce hits, trace the bounce rays.  No host synchronisation.
+ * orig/dir/maxt/hits may be pinned host memory (cudaHostAlloc or
+ * cudaHostRegister; device-addressable under unified addressing): the
+ * kernels then read the rays and write the primary hits in host memory
+ * directly, which on Grace-Blackwell runs over NVLink-C2C while the GPU
+ * traces, instead of copies before and after the frame.  The same holds for
+ * the ray and hit pointers of rta_trace. */
 int rta_frame_run(rta_frame_ctx *ctx, const rta_lbvh *bvh, const float *orig, const float *dir,
                   const float *maxt, uint32_t nrays, void *hits, uint32_t mode, uint32_t seed,
                   float eps, rta_stream_t stream);
@@ -260,6 +266,24 @@ int rta_trace_learned(const rta_lbvh *bvh, const rta_order_model *model, const f
 int rta_trace_ideal_order(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt,
                           uint32_t nrays, const void *known_hits, void *hits, uint32_t *stats,
                           rta_stream_t stream);
+
+/* Host shading on the device: lighting_collector::reset and ::shade
+ * (librta/raytrav.h:186-233), which the reference runs on the host over
+ * downloaded hits (cuda::direct_diffuse_illumination, librta/cuda.h:247-266).
+ * Writes the w*h*3-byte RGB image (row-major, as rta's image<unsigned char, 3>)
+ * byte for byte as the host shader would:
+ *   hits        w*h hit records of a primary pass (device)
+ *   tris        the 104-byte records the hits' ref indexes, i.e. the Morton-
+ *               ordered array rta_lbvh_build writes to tris_out (device;
+ *               unused when binary_only)
+ *   lights      n_lights <= 16 point lights, 6 floats each: position, colour
+ *               (host); shade() does nothing without lights
+ *   binary_only every hit pixel gets the first light's colour
+ *   background  host float[3] or NULL: reset(c) first, min(int(c*255), 255)
+ *   d_flags     optional device word: RTA_DEV_BAD_LINK if a ref is >= n_tris */
+int rta_shade_lambert(const void *hits, const void *tris, uint32_t n_tris, uint32_t w, uint32_t h,
+                      const float *lights, uint32_t n_lights, int binary_only, const float *background,
+                      void *image, uint32_t *d_flags, rta_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
 /* Batched multi-mesh build and trace                                        */

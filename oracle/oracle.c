@@ -840,3 +840,92 @@ int orc_bbvh_trace_cis(const float *nodes, const float *tris, const float *orig,
     (void)threads;
     return 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* host shading                                                               */
+/* ------------------------------------------------------------------------- */
+
+/* the conversions of lighting_collector: int(x*255) truncates toward zero */
+static int orc_to_int255(float x)
+{
+    const float v = x * 255.0f;
+    if (!(v == v)) return 0;
+    if (v >= 2147483647.0f) return 2147483647;
+    if (v <= -2147483648.0f) return (int)0x80000000u;
+    return (int)v;
+}
+
+/* barycentric_interpolation (librta/tri.h:41-48): a*b0 + b*b1, then + c*b2 */
+static void orc_bary(float out[3], const float bc[3], const float *a, const float *b, const float *c)
+{
+    for (int k = 0; k < 3; ++k) {
+        float to = a[k] * bc[0];
+        float tmp = b[k] * bc[1];
+        to = to + tmp;
+        tmp = c[k] * bc[2];
+        out[k] = to + tmp;
+    }
+}
+
+static float orc_dot3(const float *l, const float *r)
+{
+    float s = l[0] * r[0];
+    s = s + l[1] * r[1];
+    s = s + l[2] * r[2];
+    return s;
+}
+
+/* normalize_vec3f (librta/cuda-vec.h:183-188): v / sqrtf(dot(v, v)) */
+static void orc_normalize3(float v[3])
+{
+    const float len = sqrtf(orc_dot3(v, v));
+    for (int k = 0; k < 3; ++k) v[k] = v[k] / len;
+}
+
+void orc_shade_lambert(const float *tris, const orc_hit *hits, uint32_t w, uint32_t h,
+                       const float *lights, uint32_t nl, int binary, const float *bg,
+                       uint8_t *img)
+{
+    const size_t n = (size_t)w * h;
+    if (bg) {
+        /* reset (raytrav.h:189-194): min(int(c*255), 255) stored as a byte */
+        for (size_t i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k) {
+                int v = orc_to_int255(bg[k]);
+                img[3 * i + k] = (uint8_t)(v < 255 ? v : 255);
+            }
+    }
+    if (nl == 0) return;
+    for (size_t i = 0; i < n; ++i) {
+        const orc_hit *is = &hits[i];
+        if (is->t == FLT_MAX) continue;
+        float col[3] = {0.0f, 0.0f, 0.0f};
+        if (binary) {
+            col[0] = lights[3];
+            col[1] = lights[4];
+            col[2] = lights[5];
+        } else {
+            const float *tri = tris + (size_t)is->ref * 26;
+            for (uint32_t l = 0; l < nl; ++l) {
+                const float *L0 = lights + 6 * l;
+                /* triangle_intersection::barycentric_coord (basic_types.h:90-94):
+                   x = 1.0 - beta - gamma in double, stored as float */
+                const float bc[3] = {(float)(1.0 - (double)is->beta - (double)is->gamma), is->beta, is->gamma};
+                float N[3], p[3];
+                orc_bary(N, bc, tri + 9, tri + 12, tri + 15);
+                orc_bary(p, bc, tri + 0, tri + 3, tri + 6);
+                float L[3] = {L0[0] - p[0], L0[1] - p[1], L0[2] - p[2]};
+                orc_normalize3(L);
+                orc_normalize3(N);
+                float dot = orc_dot3(N, L);
+                dot = (dot < 0.0f) ? 0.0f : dot;   /* std::max(dot, 0) */
+                for (int k = 0; k < 3; ++k) col[k] = col[k] + L0[3 + k] * dot;
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            int v = orc_to_int255(col[k]);
+            v = v < 255 ? v : 255;
+            img[3 * i + k] = (uint8_t)(v > 0 ? v : 0);
+        }
+    }
+}

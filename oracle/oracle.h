@@ -127,6 +127,16 @@ int orc_bbvh_trace_cis(const float *nodes, const float *tris, const float *orig,
                        const float *dir, const float *maxt, uint32_t nrays,
                        orc_hit *hits, int threads);
 
+/* ---- host shading (librta/raytrav.h:174-243) ---- */
+
+/* lighting_collector::reset(bg) (bg may be NULL: no reset) then ::shade(binary)
+ * over the w x h hits: Lambert point lights with barycentric-interpolated
+ * vertex normals; tris are the 26-float records the hits' ref indexes;
+ * lights are nl * (position xyz, colour rgb); img is w*h*3 bytes. */
+void orc_shade_lambert(const float *tris, const orc_hit *hits, uint32_t w, uint32_t h,
+                       const float *lights, uint32_t nl, int binary, const float *bg,
+                       uint8_t *img);
+
 #ifdef __cplusplus
 }
 #endif

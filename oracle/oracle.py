@@ -64,6 +64,7 @@ def _setup(L):
     L.orc_bbvh_trace_cis.restype = i32
     L.orc_intersect_aabb.argtypes = [vp, vp, vp, vp, vp]
     L.orc_intersect_aabb.restype = i32
+    L.orc_shade_lambert.argtypes = [vp, vp, u32, u32, vp, u32, i32, vp, vp]
 
 
 class LBVH:
@@ -149,6 +150,19 @@ def diffuse_bounce(tris_sorted, orig, dirs, hits, seed, eps=1e-4):
     m = lib().orc_diffuse_bounce(_p(tris_sorted), _p(orig), _p(dirs), _p(hits), nr, seed,
                                  float(eps), _p(oo), _p(od), _p(om), _p(src))
     return oo[:3 * m], od[:3 * m], om[:m], src[:m]
+
+
+def shade_lambert(tris_sorted, hits, w, h, lights, binary=False, bg=None, img=None):
+    """lighting_collector::reset + ::shade (librta/raytrav.h:186-233); returns
+    the (h, w, 3) uint8 image.  lights: (k, 6) position xyz + colour rgb."""
+    tris_sorted = np.ascontiguousarray(tris_sorted, np.float32)
+    hits = np.ascontiguousarray(hits, HIT_DTYPE)
+    lights = np.ascontiguousarray(lights, np.float32).reshape(-1, 6)
+    out = np.zeros((h, w, 3), np.uint8) if img is None else np.array(img, np.uint8, copy=True)
+    bgp = None if bg is None else np.ascontiguousarray(bg, np.float32)
+    lib().orc_shade_lambert(_p(tris_sorted), _p(hits), w, h, _p(lights), lights.shape[0], int(bool(binary)),
+                            None if bgp is None else _p(bgp), _p(out))
+    return out
 
 
 def uniform(seed: int, index: int) -> float:

@@ -149,6 +149,11 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *tmp)
     return r;
 }
 
+// The kernel and its launcher have internal linkage: build.cu and batch.cu
+// each instantiate them, and each translation unit must launch (and set the
+// shared-memory attribute of) its own module's kernel.
+namespace {
+
 // One pass over digit bits [shift, shift + BITS).  vin == nullptr means the
 // values are the key positions (first pass).  hist is this pass's global
 // digit histogram, tstat its tile status words ([tile][radix]).  When
@@ -309,6 +314,8 @@ int sort_passes_launch(Key *k0, Key *k1, uint32_t *v0, uint32_t *v1, uint32_t n,
     *vals_sorted = vin;
     return RTA_OK;
 }
+
+} // namespace
 
 // ------------------------------------------------------------------------- //
 // Karras radix tree                                                           //

@@ -7,6 +7,7 @@
 //               counterpart), compacted in primary-ray order by a single-pass
 //               scan with decoupled look-back
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -457,4 +458,142 @@ extern "C" int rta_diffuse_bounce_noalloc(const rta_lbvh *bvh, const float *orig
     if ((rc = check_launch("k_bounce (noalloc)"))) return rc;
     RTA_CUDA_TRY(cudaMemcpyAsync(out_count, &fs->count, 4, cudaMemcpyDeviceToDevice, s));
     return RTA_OK;
+}
+
+// ------------------------------------------------------------------------- //
+// host shading on the device: lighting_collector::reset / ::shade            //
+// (librta/raytrav.h:186-233)                                                  //
+// ------------------------------------------------------------------------- //
+//
+// One thread per pixel.  Lambert point lights with barycentric-interpolated
+// vertex normals, in the reference's operation order (barycentric_coord in
+// double, basic_types.h:90-94; barycentric_interpolation, tri.h:41-48;
+// normalize_vec3f and dot_vec3f, cuda-vec.h:177-188) through round-to-nearest
+// intrinsics, so the 8-bit image equals the host shader's byte for byte.
+
+namespace rta {
+
+constexpr uint32_t kMaxLights = 16;
+
+struct ShadeLights {
+    float l[kMaxLights][6];   // position xyz, colour rgb
+    uint32_t n;
+};
+
+// int(x * 255) of the host shader (truncation; NaN -> 0, saturating)
+__device__ __forceinline__ int to_int255(float x) { return __float2int_rz(__fmul_rn(x, 255.0f)); }
+
+__device__ __forceinline__ float dot3_rn(const float *a, const float *b)
+{
+    float s = __fmul_rn(a[0], b[0]);
+    s = __fadd_rn(s, __fmul_rn(a[1], b[1]));
+    return __fadd_rn(s, __fmul_rn(a[2], b[2]));
+}
+
+__device__ __forceinline__ void normalize3_rn(float v[3])
+{
+    const float len = __fsqrt_rn(dot3_rn(v, v));
+    v[0] = __fdiv_rn(v[0], len);
+    v[1] = __fdiv_rn(v[1], len);
+    v[2] = __fdiv_rn(v[2], len);
+}
+
+__device__ __forceinline__ void bary3_rn(float out[3], const float bc[3], const float *a, const float *b,
+                                         const float *c)
+{
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        out[k] = __fadd_rn(__fadd_rn(__fmul_rn(a[k], bc[0]), __fmul_rn(b[k], bc[1])), __fmul_rn(c[k], bc[2]));
+}
+
+__global__ void k_shade_reset(uint8_t *__restrict__ img, uint32_t n, uchar3 bg)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        img[3 * (size_t)i + 0] = bg.x;
+        img[3 * (size_t)i + 1] = bg.y;
+        img[3 * (size_t)i + 2] = bg.z;
+    }
+}
+
+__global__ void k_shade_lambert(const HitRec *__restrict__ hits, const float *__restrict__ tris, uint32_t n_tris,
+                                uint32_t n, ShadeLights L, int binary, uint8_t *__restrict__ img,
+                                uint32_t *__restrict__ flags)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const HitRec is = hits[i];
+        if (is.t == FLT_MAX) continue;
+        float col[3] = {0.0f, 0.0f, 0.0f};
+        if (binary) {
+            col[0] = L.l[0][3];
+            col[1] = L.l[0][4];
+            col[2] = L.l[0][5];
+        } else {
+            if (is.ref >= n_tris) {
+                if (flags) atomicOr(flags, RTA_DEV_BAD_LINK);
+                continue;
+            }
+            const float *t = tris + (size_t)is.ref * 26;
+            float va[9], na[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                va[k] = __ldg(t + k);
+                na[k] = __ldg(t + 9 + k);
+            }
+            // x = 1.0 - beta - gamma, evaluated in double and stored as float
+            const float bc[3] = {__double2float_rn(__dsub_rn(__dsub_rn(1.0, (double)is.beta), (double)is.gamma)),
+                                 is.beta, is.gamma};
+            for (uint32_t l = 0; l < L.n; ++l) {
+                float N[3], p[3];
+                bary3_rn(N, bc, na, na + 3, na + 6);
+                bary3_rn(p, bc, va, va + 3, va + 6);
+                float D[3] = {__fsub_rn(L.l[l][0], p[0]), __fsub_rn(L.l[l][1], p[1]), __fsub_rn(L.l[l][2], p[2])};
+                normalize3_rn(D);
+                normalize3_rn(N);
+                float d = dot3_rn(N, D);
+                d = (d < 0.0f) ? 0.0f : d;   // std::max(dot, 0)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) col[k] = __fadd_rn(col[k], __fmul_rn(L.l[l][3 + k], d));
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            int v = to_int255(col[k]);
+            v = v < 255 ? v : 255;
+            img[3 * (size_t)i + k] = (uint8_t)(v > 0 ? v : 0);
+        }
+    }
+}
+
+} // namespace rta
+
+extern "C" int rta_shade_lambert(const void *hits, const void *tris, uint32_t n_tris, uint32_t w, uint32_t h,
+                                 const float *lights, uint32_t n_lights, int binary_only, const float *background,
+                                 void *image, uint32_t *d_flags, rta_stream_t stream)
+{
+    if (!hits || !image || w == 0 || h == 0 || n_lights > kMaxLights || (n_lights && !lights) ||
+        (n_lights && !binary_only && (!tris || n_tris == 0)) || (uint64_t)w * h > 0xffffffffull)
+        return RTA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t n = w * h;
+    const uint32_t blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+    if (background) {
+        // reset (raytrav.h:189-194): min(int(c * 255), 255) stored as a byte
+        unsigned char b[3];
+        for (int k = 0; k < 3; ++k) {
+            const float v = background[k] * 255.0f;
+            long iv = (v != v) ? 0 : (v >= 2147483647.0f ? 2147483647L : (v <= -2147483648.0f ? -2147483648L : (long)v));
+            b[k] = (unsigned char)(iv < 255 ? iv : 255);
+        }
+        k_shade_reset<<<blocks, 256, 0, s>>>((uint8_t *)image, n, make_uchar3(b[0], b[1], b[2]));
+        int rc = check_launch("k_shade_reset");
+        if (rc) return rc;
+    }
+    if (n_lights == 0) return RTA_OK;   // shade() returns at once without lights
+    ShadeLights L;
+    memset(&L, 0, sizeof(L));
+    memcpy(L.l, lights, (size_t)n_lights * 6 * sizeof(float));
+    L.n = n_lights;
+    k_shade_lambert<<<blocks, 256, 0, s>>>((const HitRec *)hits, (const float *)tris, n_tris, n, L, binary_only,
+                                           (uint8_t *)image, d_flags);
+    return check_launch("k_shade_lambert");
 }

@@ -67,7 +67,7 @@ class OrderModel:
     def sample(self, bvh, orig, dirs, maxt, nrays=None, d_nrays=None) -> torch.Tensor:
         """Plain trace that records decisions; returns the hits (device)."""
         n = int(nrays if nrays is not None else maxt.numel())
-        hits = torch.empty(4 * n, dtype=torch.float32, device=_dev())
+        hits = torch.zeros(4 * n, dtype=torch.float32, device=_dev())
         L.check(self.lib.rta_reset_intersections(_ptr(hits), n, 1, _stream()), "reset")
         L.check(self.lib.rta_order_sample(self.handle, C.byref(bvh.view), _ptr(orig), _ptr(dirs), _ptr(maxt),
                                           0 if d_nrays is not None else n,
@@ -109,7 +109,7 @@ class OrderModel:
     # ---- inference ----
     def trace(self, bvh, orig, dirs, maxt, stats: bool = False, nrays=None, d_nrays=None):
         n = int(nrays if nrays is not None else maxt.numel())
-        hits = torch.empty(4 * n, dtype=torch.float32, device=_dev())
+        hits = torch.zeros(4 * n, dtype=torch.float32, device=_dev())
         L.check(self.lib.rta_reset_intersections(_ptr(hits), n, 1, _stream()), "reset")
         st = torch.zeros(2 * n, dtype=torch.int32, device=_dev()) if stats else None
         L.check(self.lib.rta_trace_learned(C.byref(bvh.view), self.handle, _ptr(orig), _ptr(dirs), _ptr(maxt),
@@ -122,7 +122,7 @@ class OrderModel:
 def plain_trace(bvh, orig, dirs, maxt, stats: bool = False):
     lib = L.load()
     n = int(maxt.numel())
-    hits = torch.empty(4 * n, dtype=torch.float32, device=_dev())
+    hits = torch.zeros(4 * n, dtype=torch.float32, device=_dev())
     L.check(lib.rta_reset_intersections(_ptr(hits), n, 1, _stream()), "reset")
     st = torch.zeros(2 * n, dtype=torch.int32, device=_dev()) if stats else None
     mode = L.TRACE_CIS | (L.TRACE_STATS if stats else 0)
@@ -136,7 +136,7 @@ def ideal_trace(bvh, orig, dirs, maxt, known_hits, stats: bool = False):
     hits of an earlier trace): the bound on what a learned order can gain."""
     lib = L.load()
     n = int(maxt.numel())
-    hits = torch.empty(4 * n, dtype=torch.float32, device=_dev())
+    hits = torch.zeros(4 * n, dtype=torch.float32, device=_dev())
     L.check(lib.rta_reset_intersections(_ptr(hits), n, 1, _stream()), "reset")
     st = torch.zeros(2 * n, dtype=torch.int32, device=_dev()) if stats else None
     L.check(lib.rta_trace_ideal_order(C.byref(bvh.view), _ptr(orig), _ptr(dirs), _ptr(maxt), n, _ptr(known_hits),

@@ -28,7 +28,7 @@ SYMBOLS = [
     "rta_order_param_count", "rta_order_get_params", "rta_order_set_params", "rta_order_sample",
     "rta_order_sample_count", "rta_order_clear_samples", "rta_order_samples", "rta_order_gradient",
     "rta_order_train", "rta_trace_learned", "rta_trace_ideal_order",
-    "rta_batch_create", "rta_batch_destroy", "rta_batch_set_meshes", "rta_batch_build", "rta_batch_trace",
+    "rta_shade_lambert", "rta_batch_create", "rta_batch_destroy", "rta_batch_set_meshes", "rta_batch_build", "rta_batch_trace",
     "rta_batch_run", "rta_batch_mesh", "rta_batch_status", "rta_batch_get_params", "rta_batch_set_params",
     "rta_batch_autotune", "rta_batch_tune_key", "rta_tune_cache_lookup", "rta_tune_cache_store",
 ]
@@ -110,6 +110,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_trace_ideal_order.argtypes = [P(LbvhView), vp, vp, vp, u32, vp, vp, vp, vp]
     L.rta_diffuse_bounce_noalloc.argtypes = [P(LbvhView), vp, vp, vp, u32, u32, f32, vp, vp, vp, vp,
                                              vp, vp]
+    L.rta_shade_lambert.argtypes = [vp, vp, u32, u32, u32, vp, u32, i32, vp, vp, vp, vp]
     L.rta_batch_create.argtypes = [P(vp)]
     L.rta_batch_destroy.argtypes = [vp]
     L.rta_batch_set_meshes.argtypes = [vp, u32, vp, vp]

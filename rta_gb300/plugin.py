@@ -292,6 +292,74 @@ class primary_intersection_collector(gpu_ray_bouncer):
         return "cuda primary intersection collector."
 
 
+def write_png(filename: str, rgb: np.ndarray) -> None:
+    """An (h, w, 3) uint8 image as an 8-bit RGB PNG (zlib from the standard
+    library; rta's image<>::save_png writes the same pixels through png++)."""
+    import struct
+    import zlib
+    h, w, _ = rgb.shape
+    raw = b"".join(b"\x00" + np.ascontiguousarray(rgb[y]).tobytes() for y in range(h))
+
+    def chunk(tag, data):
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xffffffff)
+
+    with open(filename, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))
+
+
+class direct_diffuse_illumination(primary_intersection_collector):
+    """cuda::direct_diffuse_illumination (librta/cuda.h:247-266) with the
+    lighting_collector shader (librta/raytrav.h:174-243).  The reference
+    downloads every hit and shades on the host; here the shading runs on the
+    device (rta_shade_lambert) and only the 8-bit image comes back, byte for
+    byte the host shader's."""
+
+    def __init__(self, w: int, h: int):
+        super().__init__(w, h)
+        self.lights = []
+        self.triangles = None
+        self.n_tris = 0
+        self.image = torch.zeros(self.w * self.h * 3, dtype=torch.uint8, device=_dev())
+        self._bg = None
+
+    def triangle_ptr(self, tris: torch.Tensor) -> None:
+        """The Morton-ordered 104-byte records the hits index (the AS's
+        triangle_ptr(), i.e. lbvh_constructor(keep_triangles=True))."""
+        self.triangles = tris
+        self.n_tris = int(tris.numel() // TRI_FLOATS)
+
+    def add_pointlight(self, at, col) -> None:
+        self.lights.append([float(x) for x in at] + [float(x) for x in col])
+
+    def reset(self, c) -> None:
+        self._bg = np.asarray(c, np.float32)
+        self._shade(False, only_reset=True)
+
+    def shade(self, binary_result_only: bool = False) -> None:
+        self._shade(binary_result_only)
+
+    def _shade(self, binary: bool, only_reset: bool = False) -> None:
+        lights = np.asarray(self.lights, np.float32).reshape(-1, 6)
+        n = 0 if only_reset else lights.shape[0]
+        bg = self._bg if only_reset else None
+        L.check(L.load().rta_shade_lambert(_ptr(self.gpu_last_intersection), _ptr(self.triangles), self.n_tris,
+                                           self.w, self.h, lights.ctypes.data_as(C.c_void_p) if n else None, n,
+                                           int(bool(binary)), bg.ctypes.data_as(C.c_void_p) if bg is not None
+                                           else None, _ptr(self.image), None, _stream()), "rta_shade_lambert")
+
+    def pixels(self) -> np.ndarray:
+        return self.image.cpu().numpy().reshape(self.h, self.w, 3)
+
+    def save(self, filename: str) -> None:
+        write_png(filename, self.pixels())
+
+    def identification(self) -> str:
+        return "direct_diffuse_illumination shaded on the device (gb300)"
+
+
 class diffuse_bounce_collector(gpu_ray_bouncer):
     """Added bouncer: after the primary pass, one cosine-weighted diffuse
     bounce ray per hit is generated on the device and traced in the second

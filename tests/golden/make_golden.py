@@ -102,6 +102,24 @@ def ref_bbvh(tmp, tris, rays, width):
     return raw[:-4].view(np.dtype([("t", "<f4"), ("beta", "<f4"), ("gamma", "<f4"), ("id", "<u4")]))
 
 
+def ref_shade(tmp, tris, hits, w, h, lights, binary, bg):
+    """The reference's lighting_collector (librta/raytrav.h:174-243) run by
+    oracle/refbuild/shade_harness.cpp."""
+    tris.astype(np.float32).tofile(os.path.join(tmp, "st.f32"))
+    np.ascontiguousarray(hits).tofile(os.path.join(tmp, "sh.bin"))
+    lights.astype(np.float32).tofile(os.path.join(tmp, "sl.f32"))
+    r = subprocess.run([os.path.join(REFDIR, "shade_harness"), "st.f32", str(tris.shape[0]), "sh.bin", str(w),
+                        str(h), "sl.f32", str(lights.shape[0]), str(int(binary)), *map(str, bg), "img.rgb"],
+                       capture_output=True, text=True, cwd=tmp)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr)
+    return np.fromfile(os.path.join(tmp, "img.rgb"), np.uint8).reshape(h, w, 3)
+
+
+LIGHTS = np.array([[2.0, 3.0, 4.0, 0.9, 0.8, 0.7], [-3.0, 1.0, 2.0, 0.2, 0.3, 0.5]], np.float32)
+BACKGROUND = (0.1, 0.2, 0.3)
+
+
 def small_cases():
     rng = np.random.default_rng(1234)
     cases = {}
@@ -153,6 +171,16 @@ def main():
         sp["bbvh_id"] = cpu["id"]
         np.savez_compressed(os.path.join(OUT, "sphere_trace.npz"), **sp)
 
+        # host shading of that view, with the sphere's own vertex normals (same
+        # positions, so the same tree and hits)
+        smooth = S.uv_sphere()
+        lbs = ref_lbvh(tmp, smooth)
+        assert np.array_equal(lbs["ids"], lb["ids"])
+        sh = dict(lights=LIGHTS, bg=np.asarray(BACKGROUND, np.float32), tris=lbs["tris"],
+                  image=ref_shade(tmp, lbs["tris"], sp["cis_hits"], cam.w, cam.h, LIGHTS, False, BACKGROUND),
+                  binary=ref_shade(tmp, lbs["tris"], sp["cis_hits"], cam.w, cam.h, LIGHTS, True, BACKGROUND))
+        np.savez_compressed(os.path.join(OUT, "shade_sphere.npz"), **sh)
+
         # a small terrain view
         ter = records(positions(S.terrain(64, 32, seed=11)))
         lb = ref_lbvh(tmp, ter)
@@ -164,7 +192,7 @@ def main():
         for mode in ("cis", "dis"):
             tt[f"{mode}_hits"] = ref_trace(tmp, mode, lb, rays)
         np.savez_compressed(os.path.join(OUT, "terrain_trace.npz"), **tt)
-    for f in ("lbvh_cases.npz", "sphere_trace.npz", "terrain_trace.npz"):
+    for f in ("lbvh_cases.npz", "sphere_trace.npz", "terrain_trace.npz", "shade_sphere.npz"):
         print(f, os.path.getsize(os.path.join(OUT, f)))
 
 

@@ -177,3 +177,24 @@ def test_autotune_picks_valid_parameters_and_caches_them(work, tmp_path):
     b2.run(work.tris, work.orig, work.dirs, work.maxt, hits)
     assert_hits_equal(hits_np(hits), hits_np(want))
     assert os.path.getsize(cache) > 0
+
+
+@pytest.mark.parametrize("digit_bits", [8, 10, 11])
+def test_one_mesh_builds_after_batch_builds(work, digit_bits):
+    """A batch build and a one-mesh build of the same key width instantiate
+    the same sort kernel in two translation units; each must launch its own
+    (a shared launcher once left the one-mesh sort without its shared-memory
+    attribute).  Both, run back to back, match the oracle."""
+    from rta_gb300 import plugin as P
+    b = B.Batch()
+    b.set_meshes(work.tri_offsets, work.ray_offsets)
+    b.params = {"digit_bits": digit_bits}
+    b.build(work.tris)
+    tris = S.clusters(16, 1024, seed=9)
+    lb = O.lbvh_build(tris, 63)
+    ctor = P.lbvh_constructor(morton_bits=63, digit_bits=digit_bits)
+    bvh = ctor.build(P.cuda_ftl(tris))
+    np.testing.assert_array_equal(bvh.node_data_2f4().view(np.uint32), lb.nodes.view(np.uint32))
+    m = meshes_of(work) - 1
+    lbm = O.lbvh_build(work.mesh_tris(m), 30)
+    np.testing.assert_array_equal(b.mesh(m).node_data_2f4().view(np.uint32), lbm.nodes.view(np.uint32))

@@ -272,6 +272,44 @@ def test_frame_bounce_matches_oracle():
     assert_hits_equal(got_h, bref)
 
 
+def test_frame_on_pinned_host_buffers_matches_oracle():
+    """rta_frame_run with the rays and primary hits in pinned host memory
+    (read and written by the kernels directly) gives the oracle's hits and
+    bounce rays, as the device-resident frame does."""
+    import ctypes as C
+    tris = S.terrain(128, 64, seed=5)
+    cam = S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), w=320, h=180)
+    n = cam.w * cam.h
+    o, d, m = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
+    ho = torch.from_numpy(np.ascontiguousarray(o, np.float32).reshape(-1)).pin_memory()
+    hd = torch.from_numpy(np.ascontiguousarray(d, np.float32).reshape(-1)).pin_memory()
+    hm = torch.from_numpy(np.ascontiguousarray(m, np.float32).reshape(-1)).pin_memory()
+    hh = torch.zeros(4 * n, dtype=torch.float32).pin_memory()
+    bvh = gpu_build(tris, 30)
+    lib = L.load()
+    fh = C.c_void_p()
+    L.check(lib.rta_frame_create(C.byref(fh), n), "rta_frame_create")
+    try:
+        f = L.FrameView()
+        L.check(lib.rta_frame_get(fh, C.byref(f)), "rta_frame_get")
+        L.check(lib.rta_frame_run(fh, C.byref(bvh.view), P._ptr(ho), P._ptr(hd), P._ptr(hm), n, P._ptr(hh),
+                                  L.TRACE_CIS, 13, np.float32(1e-4), P._stream()), "rta_frame_run")
+        torch.cuda.synchronize()
+        lb = O.lbvh_build(tris, 30)
+        srt = O.permute(tris, lb.ids)
+        ref, _, _ = O.trace(lb.nodes, srt, o, d, m, O.CIS, 64)
+        assert_hits_equal(hh.numpy().view(O.HIT_DTYPE), ref)
+        bo, bd, bm, bsrc = O.diffuse_bounce(srt, o, d, ref, seed=13, eps=1e-4)
+        cnt = int(P.device_view(f.count, 1, "<u4").cpu().numpy().view(np.uint32)[0])
+        assert cnt == bm.shape[0] and cnt > 0
+        got_o = P.device_view(f.orig, 3 * cnt).cpu().numpy()
+        np.testing.assert_array_equal(got_o.view(np.uint32), bo.view(np.uint32))
+        bref, _, _ = O.trace(lb.nodes, srt, bo, bd, bm, O.CIS, 64)
+        assert_hits_equal(P.device_view(f.hits, 4 * cnt).cpu().numpy().view(O.HIT_DTYPE), bref)
+    finally:
+        lib.rta_frame_destroy(fh)
+
+
 def test_rebinding_contract():
     """rt.acceleration_structure(new_as) makes the tracer use the new tree
     (bbvh-cuda.h:89-92, rta/main.cpp:389-400)."""
@@ -303,3 +341,83 @@ def test_full_size_terrain_build_and_frame():
     srt = O.permute(tris, lb.ids)
     ref, _, _ = O.trace(lb.nodes, srt, o, d, m, O.CIS, 64)
     assert_hits_equal(gpu_trace(bvh, o, d, m, L.TRACE_CIS), ref)
+
+
+def test_full_size_incoherent_clusters_build_and_trace():
+    """The 4,194,304-triangle cluster soup with 63-bit codes and 8,388,608
+    incoherent rays: tree and every hit bit-identical to the oracle's, and
+    the closest-hit trace of a quarter of the rays in the DIS order too."""
+    tris = S.clusters(256, 16384, seed=0)
+    lb = O.lbvh_build(tris, 63)
+    bvh = gpu_build(tris, 63)
+    assert (np.diff(bvh.codes().astype(np.float64)) >= 0).all()
+    assert_build_equals(bvh, lb.codes, lb.ids, lb.nodes)
+    o, d, m = S.incoherent_rays(1 << 23, seed=0)
+    srt = O.permute(tris, lb.ids)
+    ref, st_ref, overflow = O.trace(lb.nodes, srt, o, d, m, O.CIS, 128, stats=True)
+    assert not overflow
+    got, st = gpu_trace(bvh, o, d, m, L.TRACE_CIS, stats=True)
+    assert_hits_equal(got, ref)
+    np.testing.assert_array_equal(st, st_ref)   # same nodes and triangles visited per ray
+    q = slice(0, 1 << 21)
+    ref_dis, _, _ = O.trace(lb.nodes, srt, o.reshape(-1, 3)[q], d.reshape(-1, 3)[q], m[q], O.DIS, 128)
+    assert_hits_equal(gpu_trace(bvh, o.reshape(-1, 3)[q], d.reshape(-1, 3)[q], m[q], L.TRACE_DIS), ref_dis)
+    assert bvh.status() & (L.DEV_STACK_OVERFLOW | L.DEV_ITER_LIMIT | L.DEV_BAD_LINK | L.DEV_SPIN_TIMEOUT) == 0
+
+
+# --------------------------------------------------------------------------- #
+# host shading on the device                                                  #
+# --------------------------------------------------------------------------- #
+
+def gpu_shade(hits, tris, w, h, lights, binary, bg):
+    import ctypes as C
+    dev = torch.device("cuda")
+    hd = torch.from_numpy(np.ascontiguousarray(hits).view(np.float32).reshape(-1).copy()).to(dev)
+    td = torch.from_numpy(np.ascontiguousarray(tris, np.float32).reshape(-1).copy()).to(dev)
+    img = torch.zeros(w * h * 3, dtype=torch.uint8, device=dev)
+    lt = np.ascontiguousarray(lights, np.float32)
+    bgv = np.ascontiguousarray(bg, np.float32)
+    flags = torch.zeros(1, dtype=torch.int32, device=dev)
+    L.check(L.load().rta_shade_lambert(P._ptr(hd), P._ptr(td), tris.shape[0], w, h,
+                                       lt.ctypes.data_as(C.c_void_p), lt.shape[0], int(binary),
+                                       bgv.ctypes.data_as(C.c_void_p), P._ptr(img), P._ptr(flags),
+                                       P._stream()), "rta_shade_lambert")
+    torch.cuda.synchronize()
+    assert int(flags.item()) == 0
+    return img.cpu().numpy().reshape(h, w, 3)
+
+
+def test_shading_matches_reference_golden(golden_dir):
+    z = np.load(os.path.join(golden_dir, "shade_sphere.npz"))
+    sp = np.load(os.path.join(golden_dir, "sphere_trace.npz"))
+    w, h = int(sp["w"]), int(sp["h"])
+    hits = sp["cis_hits"].view(O.HIT_DTYPE)
+    np.testing.assert_array_equal(gpu_shade(hits, z["tris"], w, h, z["lights"], False, z["bg"]), z["image"])
+    np.testing.assert_array_equal(gpu_shade(hits, z["tris"], w, h, z["lights"], True, z["bg"]), z["binary"])
+
+
+def test_direct_diffuse_illumination_full_frame_matches_oracle(tmp_path):
+    """The terrain's 1920x1080 primary frame shaded on the device through the
+    plugin mirror (trace, then shade) equals the oracle's host shading."""
+    tris = S.terrain(1024, 512, seed=0)
+    s = P.create_rt_set(tris, 1920, 1080)
+    cam = S.terrain_camera()
+    s.rgen.setup(cam.pos, cam.dir, cam.up, cam.fovy)
+    shader = P.direct_diffuse_illumination(1920, 1080)
+    s.rt.ray_generator(s.rgen)
+    s.rt.ray_bouncer(shader)
+    s.rt.trace()
+    shader.triangle_ptr(s.as_.triangle_data)
+    lights = [((1.5, 2.0, 1.0), (0.8, 0.75, 0.7)), ((-1.0, 1.0, -0.5), (0.2, 0.25, 0.35))]
+    shader.reset((0.05, 0.1, 0.2))
+    for at, col in lights:
+        shader.add_pointlight(at, col)
+    shader.shade()
+    got = shader.pixels()
+    hits = shader.intersections()
+    want = O.shade_lambert(s.as_.canonical_triangle_ptr(), hits, 1920, 1080,
+                           np.array([list(a) + list(c) for a, c in lights], np.float32), False, (0.05, 0.1, 0.2))
+    np.testing.assert_array_equal(got, want)
+    path = str(tmp_path / "frame.png")
+    shader.save(path)
+    assert os.path.getsize(path) > 1000

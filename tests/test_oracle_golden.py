@@ -131,3 +131,38 @@ def test_terrain_trace_matches_reference(golden_dir, mode):
     hits, _, _ = O.trace(lb.nodes, srt, o, d, m, MODES[mode], stack_limit=32)
     ref = z[f"{mode}_hits"]
     assert sha(hits) == sha(ref)
+
+
+def test_shading_matches_reference_lighting_collector(golden_dir):
+    """orc_shade_lambert against the reference's own lighting_collector
+    (librta/raytrav.h:174-243) run on the sphere view's hits."""
+    z = np.load(os.path.join(golden_dir, "shade_sphere.npz"))
+    sp = np.load(os.path.join(golden_dir, "sphere_trace.npz"))
+    hits = sp["cis_hits"].view(O.HIT_DTYPE)
+    w, h = int(sp["w"]), int(sp["h"])
+    img = O.shade_lambert(z["tris"], hits, w, h, z["lights"], False, z["bg"])
+    np.testing.assert_array_equal(img, z["image"])
+    img = O.shade_lambert(z["tris"], hits, w, h, z["lights"], True, z["bg"])
+    np.testing.assert_array_equal(img, z["binary"])
+    # the background of reset(c) on every miss, shading on every hit
+    miss = hits["t"] == np.float32(np.finfo(np.float32).max)
+    assert np.all(z["image"][miss.reshape(h, w)] == np.array([25, 51, 76], np.uint8))
+    assert (~miss).sum() > 10000
+
+
+def test_png_writer_round_trip(tmp_path):
+    import struct
+    import zlib
+    from rta_gb300.plugin import write_png
+    rgb = np.random.default_rng(0).integers(0, 256, size=(7, 5, 3), dtype=np.uint8)
+    path = str(tmp_path / "x.png")
+    write_png(path, rgb)
+    data = open(path, "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    w, h = struct.unpack(">II", data[16:24])
+    assert (w, h) == (5, 7)
+    idat_len = struct.unpack(">I", data[33:37])[0]
+    raw = zlib.decompress(data[41:41 + idat_len])
+    rows = np.frombuffer(raw, np.uint8).reshape(7, 1 + 5 * 3)
+    assert np.all(rows[:, 0] == 0)
+    np.testing.assert_array_equal(rows[:, 1:].reshape(7, 5, 3), rgb)
