@@ -176,18 +176,36 @@ int rta_diffuse_bounce(rta_frame_ctx *ctx, const rta_lbvh *bvh, const float *ori
 
 /* Whole frame: reset primary hits, trace primary rays, generate the bounce,
  * reset bounce hits, trace the bounce rays.  No host synchronisation.
- * orig/dir/maxt/hits may be pinned host memory (cudaHostAlloc or
- * cudaHostRegister; device-addressable under unified addressing): the
- * kernels then read the rays and write the primary hits in host memory
- * directly, which on Grace-Blackwell runs over NVLink-C2C while the GPU
- * traces, instead of copies before and after the frame.  The same holds for
- * the ray and hit pointers of rta_trace. */
+ * orig/dir/maxt/hits are device-addressable: device memory, or pinned host
+ * memory under unified addressing (then read and written over the host
+ * link; for frames on host buffers rta_host_frames_run is faster). */
 int rta_frame_run(rta_frame_ctx *ctx, const rta_lbvh *bvh, const float *orig, const float *dir,
                   const float *maxt, uint32_t nrays, void *hits, uint32_t mode, uint32_t seed,
                   float eps, rta_stream_t stream);
 
 /* Synchronises and returns the frame's device status flags. */
 int rta_frame_status(rta_frame_ctx *ctx, rta_stream_t stream, uint32_t *flags);
+
+/* Frames on host buffers (no counterpart in the reference, whose frames
+ * start and end in device memory; its driver downloads the hits, see
+ * primary_intersection_downloader, librta/cuda.h:222-245).  Each run copies
+ * the rays in, runs rta_frame_run and copies the primary hits, the bounce
+ * hits and the bounce count out, on three internal streams with two sets of
+ * device buffers used in turn, so consecutive calls overlap one frame's
+ * copies with the neighbouring frames' traversal.  Host pointers must be
+ * pinned (cudaHostAlloc / cudaHostRegister).  The rays must be in host memory
+ * when the call is made; the outputs are complete once `stream` passes the
+ * point where the call left it (the call makes `stream` wait for them).
+ * h_bounce_hits needs room for nrays records; *h_bounce_count receives the
+ * number written.  Two frames may be in flight; a third waits on the GPU for
+ * its buffers, not on the host. */
+typedef struct rta_host_frames rta_host_frames;
+int rta_host_frames_create(rta_host_frames **out, uint32_t max_rays);
+int rta_host_frames_destroy(rta_host_frames *frames);
+int rta_host_frames_run(rta_host_frames *frames, const rta_lbvh *bvh, const float *h_orig,
+                        const float *h_dir, const float *h_maxt, uint32_t nrays, void *h_hits,
+                        void *h_bounce_hits, uint32_t *h_bounce_count, uint32_t mode, uint32_t seed,
+                        float eps, rta_stream_t stream);
 
 /* No counterpart in the reference.  rta_diffuse_bounce for callers that may
  * not allocate device memory: a renderer that hands all device memory to its

@@ -597,3 +597,148 @@ extern "C" int rta_shade_lambert(const void *hits, const void *tris, uint32_t n_
                                            (uint8_t *)image, d_flags);
     return check_launch("k_shade_lambert");
 }
+
+// ------------------------------------------------------------------------- //
+// frames on host buffers, pipelined                                          //
+// ------------------------------------------------------------------------- //
+//
+// A renderer that keeps its rays and hits in host memory calls one frame
+// after another.  Each call copies its rays in on one stream, traces the
+// frame (rta_frame_run) on a second, and copies its hits out on a third,
+// with two sets of device buffers used in turn, so that the copies of one
+// frame overlap the traversal of its neighbours:
+//
+//   h2d    H2D rays(k)                       H2D rays(k+1)
+//   comp                 frame(k)                            frame(k+1)
+//   d2h                            D2H hits(k)                          ...
+//
+// Events order the three streams: frame k waits for its rays; the rays of
+// frame k+2 (same buffers as k) wait until frame k's hits are out.
+
+namespace rta {
+
+// the `count` bounce hits of a frame into host memory (device-addressable
+// pinned memory, written over the host link)
+__global__ void k_copy_bounce_hits(const HitRec *__restrict__ src, const uint32_t *__restrict__ count,
+                                   uint32_t cap, float4 *__restrict__ dst)
+{
+    const uint32_t n = min(*count, cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        dst[i] = reinterpret_cast<const float4 *>(src)[i];
+}
+
+} // namespace rta
+
+struct rta_host_frames {
+    uint32_t cap = 0;
+    rta_frame_ctx *slot[2] = {nullptr, nullptr};
+    float *orig[2] = {nullptr, nullptr}, *dir[2] = {nullptr, nullptr}, *maxt[2] = {nullptr, nullptr};
+    HitRec *hits[2] = {nullptr, nullptr};
+    cudaStream_t h2d = nullptr, comp = nullptr, d2h = nullptr;
+    cudaEvent_t in_done[2] = {nullptr, nullptr}, comp_done[2] = {nullptr, nullptr}, out_done[2] = {nullptr, nullptr};
+    bool used[2] = {false, false};
+    uint32_t next = 0;
+};
+
+static void free_host_frames(rta_host_frames *p)
+{
+    for (int k = 0; k < 2; ++k) {
+        if (p->slot[k]) rta_frame_destroy(p->slot[k]);
+        void *ptrs[] = {p->orig[k], p->dir[k], p->maxt[k], p->hits[k]};
+        for (void *q : ptrs)
+            if (q) cudaFree(q);
+        cudaEvent_t evs[] = {p->in_done[k], p->comp_done[k], p->out_done[k]};
+        for (cudaEvent_t e : evs)
+            if (e) cudaEventDestroy(e);
+    }
+    cudaStream_t ss[] = {p->h2d, p->comp, p->d2h};
+    for (cudaStream_t s : ss)
+        if (s) cudaStreamDestroy(s);
+}
+
+extern "C" {
+
+int rta_host_frames_create(rta_host_frames **out, uint32_t max_rays)
+{
+    if (!out || max_rays == 0) return RTA_ERR_INVALID;
+    rta_host_frames *p = new rta_host_frames();
+    p->cap = max_rays;
+    auto fail = [&](int rc) {
+        free_host_frames(p);
+        delete p;
+        return rc;
+    };
+    int rc;
+    for (int k = 0; k < 2; ++k) {
+        if ((rc = rta_frame_create(&p->slot[k], max_rays))) return fail(rc);
+        cudaError_t e = cudaSuccess;
+        if (e == cudaSuccess) e = cudaMalloc(&p->orig[k], (size_t)max_rays * 12);
+        if (e == cudaSuccess) e = cudaMalloc(&p->dir[k], (size_t)max_rays * 12);
+        if (e == cudaSuccess) e = cudaMalloc(&p->maxt[k], (size_t)max_rays * 4);
+        if (e == cudaSuccess) e = cudaMalloc(&p->hits[k], (size_t)max_rays * sizeof(HitRec));
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->in_done[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->comp_done[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->out_done[k], cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            set_cuda_error(e, "rta_host_frames_create");
+            return fail(e == cudaErrorMemoryAllocation ? RTA_ERR_NOMEM : RTA_ERR_CUDA);
+        }
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&p->h2d, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->comp, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->d2h, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "rta_host_frames_create");
+        return fail(RTA_ERR_CUDA);
+    }
+    *out = p;
+    return RTA_OK;
+}
+
+int rta_host_frames_destroy(rta_host_frames *p)
+{
+    if (!p) return RTA_ERR_INVALID;
+    cudaStreamSynchronize(p->h2d);
+    cudaStreamSynchronize(p->comp);
+    cudaStreamSynchronize(p->d2h);
+    free_host_frames(p);
+    delete p;
+    return RTA_OK;
+}
+
+int rta_host_frames_run(rta_host_frames *p, const rta_lbvh *bvh, const float *h_orig, const float *h_dir,
+                        const float *h_maxt, uint32_t nrays, void *h_hits, void *h_bounce_hits,
+                        uint32_t *h_bounce_count, uint32_t mode, uint32_t seed, float eps, rta_stream_t stream)
+{
+    if (!p || !bvh || !h_orig || !h_dir || !h_maxt || !h_hits || !h_bounce_hits || !h_bounce_count || nrays == 0 ||
+        nrays > p->cap)
+        return RTA_ERR_INVALID;
+    const uint32_t k = p->next;
+    p->next ^= 1u;
+    rta_frame_ctx *f = p->slot[k];
+    // rays in, once frame k-2's hits (same buffers) are out
+    if (p->used[k]) RTA_CUDA_TRY(cudaStreamWaitEvent(p->h2d, p->out_done[k], 0));
+    RTA_CUDA_TRY(cudaMemcpyAsync(p->orig[k], h_orig, (size_t)nrays * 12, cudaMemcpyHostToDevice, p->h2d));
+    RTA_CUDA_TRY(cudaMemcpyAsync(p->dir[k], h_dir, (size_t)nrays * 12, cudaMemcpyHostToDevice, p->h2d));
+    RTA_CUDA_TRY(cudaMemcpyAsync(p->maxt[k], h_maxt, (size_t)nrays * 4, cudaMemcpyHostToDevice, p->h2d));
+    RTA_CUDA_TRY(cudaEventRecord(p->in_done[k], p->h2d));
+    // the frame
+    RTA_CUDA_TRY(cudaStreamWaitEvent(p->comp, p->in_done[k], 0));
+    int rc = rta_frame_run(f, bvh, p->orig[k], p->dir[k], p->maxt[k], nrays, p->hits[k], mode, seed, eps, p->comp);
+    if (rc) return rc;
+    RTA_CUDA_TRY(cudaEventRecord(p->comp_done[k], p->comp));
+    // hits out
+    RTA_CUDA_TRY(cudaStreamWaitEvent(p->d2h, p->comp_done[k], 0));
+    RTA_CUDA_TRY(cudaMemcpyAsync(h_hits, p->hits[k], (size_t)nrays * sizeof(HitRec), cudaMemcpyDeviceToHost, p->d2h));
+    RTA_CUDA_TRY(cudaMemcpyAsync(h_bounce_count, &f->fs->count, 4, cudaMemcpyDeviceToHost, p->d2h));
+    const uint32_t blocks = (nrays + 255) / 256 < 1024 ? (nrays + 255) / 256 : 1024;
+    k_copy_bounce_hits<<<blocks, 256, 0, p->d2h>>>(f->hits, &f->fs->count, nrays, (float4 *)h_bounce_hits);
+    if ((rc = check_launch("k_copy_bounce_hits"))) return rc;
+    RTA_CUDA_TRY(cudaEventRecord(p->out_done[k], p->d2h));
+    p->used[k] = true;
+    // the caller's stream sees this frame's results once it passes here
+    RTA_CUDA_TRY(cudaStreamWaitEvent((cudaStream_t)stream, p->out_done[k], 0));
+    return RTA_OK;
+}
+
+} // extern "C"

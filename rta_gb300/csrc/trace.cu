@@ -38,16 +38,22 @@ struct Ray {
     float o[3], d[3];
     uint32_t zero;   // bit k: d[k] == 0
     float tmax;
+    float rd[3];     // RN(1 / d[k]) for the slab filter
+    bool fast;       // the slab filter applies (every nonzero |d[k]| in [2^-100, 2^100])
 };
 
 __device__ __forceinline__ void make_ray(Ray &R, const float o[3], const float d[3], float tmax)
 {
     R.zero = 0;
+    R.fast = true;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         R.o[k] = o[k];
         R.d[k] = d[k];
         if (d[k] == 0.0f) R.zero |= 1u << k;
+        const float ad = fabsf(d[k]);
+        R.fast = R.fast && (d[k] == 0.0f || (ad >= 7.8886091e-31f && ad <= 1.2676506e30f));
+        R.rd[k] = d[k] == 0.0f ? 0.0f : __frcp_rn(d[k]);
     }
     R.tmax = tmax;
 }
@@ -84,6 +90,92 @@ __device__ __forceinline__ bool slab_test(float lx, float hx, float ly, float hy
 {
     float far;
     return slab_test(lx, hx, ly, hy, lz, hz, R, dist, far);
+}
+
+// ---- exact slab decisions without divisions, where they are certain ----
+//
+// The child-is step needs only decisions from the slab test: does each child
+// count as hit (inside, t_near <= t_far, t_far >= 0, and not culled:
+// t_near < best t, t_near <= t_max), and is the left t_near <= the right one.
+// With r = RN(1/d) and q = RN(a * r) each quotient is within |q| * 2^-22 of
+// RN(a / d) (two roundings of 2^-24 relative each against one), for normal
+// results; 2^-146 absolute covers subnormal ones.  t_near is a max and t_far
+// a min of such quotients, so the exact t_near / t_far lie within
+// |t| * 2^-21 + 2^-146 of the approximate ones (the bound of the quotient
+// that attains the max or min dominates every other's).  The bounds are
+// rounded outward.  A decision is taken from the intervals when it is the
+// same for every value in them; otherwise the step falls back to the exact
+// divisions.  NaN bounds (overflowing quotients) always count as uncertain.
+#ifndef RTA_SLAB_FILTER
+#define RTA_SLAB_FILTER 1
+#endif
+constexpr float kFilterRel = 4.76837158e-07f;   // 2^-21
+constexpr float kFilterAbs = 1.12103877e-44f;   // 2^-146
+
+// 0: certainly not a kept hit; 1: certainly a kept hit; 2: uncertain.
+// [lo, hi] bounds the exact t_near when the child is kept.
+__device__ __forceinline__ int slab_filter(float lx, float hx, float ly, float hy, float lz, float hz,
+                                           const Ray &R, float best_t, float &lo, float &hi)
+{
+    const float bl[3] = {lx, ly, lz}, bh[3] = {hx, hy, hz};
+    float tn = -FLT_MAX, tf = FLT_MAX;
+    bool inside = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (R.zero & (1u << k)) {
+            inside = inside && !(R.o[k] < bl[k] || R.o[k] > bh[k]);
+        } else {
+            const float q1 = __fmul_rn(__fsub_rn(bl[k], R.o[k]), R.rd[k]);
+            const float q2 = __fmul_rn(__fsub_rn(bh[k], R.o[k]), R.rd[k]);
+            tn = fmaxf(tn, fminf(q1, q2));
+            tf = fminf(tf, fmaxf(q1, q2));
+        }
+    }
+    if (!inside) return 0;
+    const float wn = __fmaf_ru(fabsf(tn), kFilterRel, kFilterAbs);
+    const float wf = __fmaf_ru(fabsf(tf), kFilterRel, kFilterAbs);
+    const float tn_lo = __fsub_rd(tn, wn), tn_hi = __fadd_ru(tn, wn);
+    const float tf_lo = __fsub_rd(tf, wf), tf_hi = __fadd_ru(tf, wf);
+    // hit = t_near <= t_far && t_far >= 0; kept = hit && !(t_near >= best_t) && !(t_near > t_max)
+    if (tn_lo > tf_hi || tf_hi < 0.0f || tn_lo >= best_t || tn_lo > R.tmax) return 0;   // certainly not
+    lo = tn_lo;
+    hi = tn_hi;
+    if (tn_hi <= tf_lo && tf_lo >= 0.0f && tn_hi < best_t && tn_hi <= R.tmax) return 1;  // certainly
+    return 2;
+}
+
+// The child-is decisions of one node: hl / hr (child hit and not culled) and
+// left_first (dl <= dr); exact, through the filter where it is certain.
+__device__ __forceinline__ void cis_decide(const NodeRec &nd, const Ray &R, float best_t, bool &hl, bool &hr,
+                                           bool &left_first)
+{
+    if (RTA_SLAB_FILTER && R.fast) {
+        float llo = 0.f, lhi = 0.f, rlo = 0.f, rhi = 0.f;
+        const int sl = slab_filter(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, best_t, llo, lhi);
+        const int sr = slab_filter(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, best_t, rlo, rhi);
+        if (sl != 2 && sr != 2) {
+            hl = sl == 1;
+            hr = sr == 1;
+            if (!(hl && hr)) {
+                left_first = true;
+                return;
+            }
+            if (lhi <= rlo) {
+                left_first = true;
+                return;
+            }
+            if (llo > rhi) {
+                left_first = false;
+                return;
+            }
+        }
+    }
+    float dl = FLT_MAX, dr = FLT_MAX;
+    hl = slab_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, dl);
+    hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, dr);
+    if (dl >= best_t || dl > R.tmax) hl = false;
+    if (dr >= best_t || dr > R.tmax) hr = false;
+    left_first = dl <= dr;
 }
 
 // intersect_aabb_aila with the ailabox kernels' reciprocal (kernels.cu:966-970)
@@ -302,18 +394,17 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(TraceArgs A)
                 } else {
                     ++inner_visits;
                     const NodeRec nd = load_node(A.nodes, cur);
-                    float dl = FLT_MAX, dr = FLT_MAX;
-                    bool hl, hr;
+                    bool hl, hr, left_first;
                     if (AILA) {
+                        float dl = FLT_MAX, dr = FLT_MAX;
                         hl = aila_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R.o, id, best.t, dl);
                         hr = aila_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R.o, id, best.t, dr);
+                        if (dl >= best.t || dl > R.tmax) hl = false;
+                        if (dr >= best.t || dr > R.tmax) hr = false;
+                        left_first = dl <= dr;
                     } else {
-                        hl = slab_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, dl);
-                        hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, dr);
+                        cis_decide(nd, R, best.t, hl, hr, left_first);
                     }
-                    if (dl >= best.t || dl > R.tmax) hl = false;
-                    if (dr >= best.t || dr > R.tmax) hr = false;
-                    const bool left_first = dl <= dr;
                     if (hl && hr) {
                         if (sp + 1 >= STACK) {
                             overflow = true;
@@ -500,16 +591,13 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_batch(BatchTraceArgs A)
             } else {
                 ++inner_visits;
                 const NodeRec nd = load_node(nodes, cur);
-                float dl = FLT_MAX, dr = FLT_MAX;
-                bool hl = slab_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, dl);
-                bool hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, dr);
-                if (dl >= best.t || dl > R.tmax) hl = false;
-                if (dr >= best.t || dr > R.tmax) hr = false;
+                bool hl, hr, left_first;
+                cis_decide(nd, R, best.t, hl, hr, left_first);
                 if (hl && hr) {
                     if (sp + 1 >= STACK) {
                         overflow = true;
                         done = true;
-                    } else if (dl <= dr) {
+                    } else if (left_first) {
                         stack[++sp] = nd.q3.y;
                         cur = nd.q3.x;
                     } else {

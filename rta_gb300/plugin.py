@@ -292,6 +292,34 @@ class primary_intersection_collector(gpu_ray_bouncer):
         return "cuda primary intersection collector."
 
 
+class host_frames:
+    """rta_host_frames: frames whose rays and hits live in pinned host
+    memory, pipelined so that one frame's copies overlap the neighbouring
+    frames' traversal (two frames in flight)."""
+
+    def __init__(self, max_rays: int):
+        self.lib = L.load()
+        h = C.c_void_p()
+        L.check(self.lib.rta_host_frames_create(C.byref(h), int(max_rays)), "rta_host_frames_create")
+        self.handle = h
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            try:
+                self.lib.rta_host_frames_destroy(self.handle)
+            except Exception:
+                pass
+            self.handle = None
+
+    def run(self, bvh, h_orig, h_dir, h_maxt, h_hits, h_bounce_hits, h_bounce_count, mode=L.TRACE_CIS,
+            seed: int = 0, eps: float = 1e-4, nrays=None) -> None:
+        n = int(h_maxt.numel() if nrays is None else nrays)
+        L.check(self.lib.rta_host_frames_run(self.handle, C.byref(bvh.view), _ptr(h_orig), _ptr(h_dir),
+                                             _ptr(h_maxt), n, _ptr(h_hits), _ptr(h_bounce_hits),
+                                             _ptr(h_bounce_count), mode, seed, float(eps), _stream()),
+                "rta_host_frames_run")
+
+
 def write_png(filename: str, rgb: np.ndarray) -> None:
     """An (h, w, 3) uint8 image as an 8-bit RGB PNG (zlib from the standard
     library; rta's image<>::save_png writes the same pixels through png++)."""

@@ -421,3 +421,50 @@ def test_direct_diffuse_illumination_full_frame_matches_oracle(tmp_path):
     path = str(tmp_path / "frame.png")
     shader.save(path)
     assert os.path.getsize(path) > 1000
+
+
+def test_host_frames_pipeline_matches_device_frames():
+    """Three frames in a row through rta_host_frames_run (pinned host
+    buffers, two frames in flight) equal rta_frame_run on device buffers,
+    primary and bounce hits and bounce counts, each frame with its own seed
+    and its own output buffers."""
+    import ctypes as C
+    tris = S.terrain(128, 64, seed=5)
+    cam = S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), w=320, h=180)
+    n = cam.w * cam.h
+    o, d, m = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
+    ho = torch.from_numpy(np.ascontiguousarray(o, np.float32).reshape(-1)).pin_memory()
+    hd = torch.from_numpy(np.ascontiguousarray(d, np.float32).reshape(-1)).pin_memory()
+    hm = torch.from_numpy(np.ascontiguousarray(m, np.float32).reshape(-1)).pin_memory()
+    bvh = gpu_build(tris, 30)
+    hf = P.host_frames(n)
+    outs = []
+    for seed in (3, 4, 5):
+        hh = torch.zeros(4 * n, dtype=torch.float32).pin_memory()
+        hb = torch.zeros(4 * n, dtype=torch.float32).pin_memory()
+        hc = torch.zeros(1, dtype=torch.int32).pin_memory()
+        hf.run(bvh, ho, hd, hm, hh, hb, hc, L.TRACE_CIS, seed, 1e-4)
+        outs.append((seed, hh, hb, hc))
+    torch.cuda.current_stream().synchronize()
+    lib = L.load()
+    dev = torch.device("cuda")
+    do, dd, dm = ho.to(dev), hd.to(dev), hm.to(dev)
+    for seed, hh, hb, hc in outs:
+        fh = C.c_void_p()
+        L.check(lib.rta_frame_create(C.byref(fh), n), "rta_frame_create")
+        f = L.FrameView()
+        L.check(lib.rta_frame_get(fh, C.byref(f)), "rta_frame_get")
+        dh = torch.zeros(4 * n, dtype=torch.float32, device=dev)
+        L.check(lib.rta_frame_run(fh, C.byref(bvh.view), P._ptr(do), P._ptr(dd), P._ptr(dm), n, P._ptr(dh),
+                                  L.TRACE_CIS, seed, np.float32(1e-4), P._stream()), "rta_frame_run")
+        torch.cuda.synchronize()
+        cnt = int(P.device_view(f.count, 1, "<u4").cpu().numpy().view(np.uint32)[0])
+        assert int(hc.item()) == cnt > 0
+        assert_hits_equal(hh.numpy().view(O.HIT_DTYPE), dh.cpu().numpy().view(O.HIT_DTYPE))
+        want_b = P.device_view(f.hits, 4 * cnt).cpu().numpy().view(O.HIT_DTYPE)
+        got_b = hb.numpy().view(O.HIT_DTYPE)[:cnt]
+        np.testing.assert_array_equal(got_b["t"].view(np.uint32), want_b["t"].view(np.uint32))
+        v = got_b["t"] != np.float32(S.FLT_MAX)
+        for fld in ("beta", "gamma", "ref"):
+            np.testing.assert_array_equal(got_b[fld][v].view(np.uint32), want_b[fld][v].view(np.uint32))
+        lib.rta_frame_destroy(fh)
