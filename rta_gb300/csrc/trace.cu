@@ -144,6 +144,51 @@ __device__ __forceinline__ int slab_filter(float lx, float hx, float ly, float h
     return 2;
 }
 
+// The entry distance of one box from its near planes: the approximate
+// quotient of every axis, the axis that attains the max, and whether that
+// axis certainly attains the exact max too (every other axis' exact quotient
+// is certainly smaller).  Then the exact entry distance is
+// RN((plane - o) / d) of that one axis; `num` is its numerator plane - o and
+// `den` its d.  (Selects, not indexing: a run-time index would put the ray
+// into local memory.)
+__device__ __forceinline__ bool entry_axis(float lx, float hx, float ly, float hy, float lz, float hz,
+                                           const Ray &R, int &axis, float &plane, float &num, float &den)
+{
+    const float c0 = R.d[0] > 0.0f ? lx : hx, c1 = R.d[1] > 0.0f ? ly : hy, c2 = R.d[2] > 0.0f ? lz : hz;
+    const float a0 = __fsub_rn(c0, R.o[0]), a1 = __fsub_rn(c1, R.o[1]), a2 = __fsub_rn(c2, R.o[2]);
+    const float q0 = (R.zero & 1u) ? -FLT_MAX : __fmul_rn(a0, R.rd[0]);
+    const float q1 = (R.zero & 2u) ? -FLT_MAX : __fmul_rn(a1, R.rd[1]);
+    const float q2 = (R.zero & 4u) ? -FLT_MAX : __fmul_rn(a2, R.rd[2]);
+    const bool k2 = q2 >= fmaxf(q0, q1);
+    const bool k1 = !k2 && q1 >= q0;
+    const float top = k2 ? q2 : (k1 ? q1 : q0);
+    const float second = k2 ? fmaxf(q0, q1) : (k1 ? fmaxf(q0, q2) : fmaxf(q1, q2));
+    axis = k2 ? 2 : (k1 ? 1 : 0);
+    plane = k2 ? c2 : (k1 ? c1 : c0);
+    num = k2 ? a2 : (k1 ? a1 : a0);
+    den = k2 ? R.d[2] : (k1 ? R.d[1] : R.d[0]);
+    const float wt = __fmaf_ru(fabsf(top), kFilterRel, kFilterAbs);
+    const float ws = __fmaf_ru(fabsf(second), kFilterRel, kFilterAbs);
+    return top != -FLT_MAX && __fadd_ru(second, ws) < __fsub_rd(top, wt);
+}
+
+// dl <= dr for two kept children whose entry intervals overlap: equal planes
+// give equal quotients (the reference then goes left); otherwise one exact
+// division per child.  Returns false when an entry axis is not certain.
+__device__ __forceinline__ bool order_resolve(const NodeRec &nd, const Ray &R, bool &left_first)
+{
+    int kl, kr;
+    float cl, cr, nl, nr, dl_den, dr_den;
+    if (!entry_axis(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, kl, cl, nl, dl_den)) return false;
+    if (!entry_axis(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, kr, cr, nr, dr_den)) return false;
+    if (kl == kr && __float_as_uint(cl) == __float_as_uint(cr)) {
+        left_first = true;
+        return true;
+    }
+    left_first = __fdiv_rn(nl, dl_den) <= __fdiv_rn(nr, dr_den);
+    return true;
+}
+
 // The child-is decisions of one node: hl / hr (child hit and not culled) and
 // left_first (dl <= dr); exact, through the filter where it is certain.
 __device__ __forceinline__ void cis_decide(const NodeRec &nd, const Ray &R, float best_t, bool &hl, bool &hr,
@@ -168,6 +213,7 @@ __device__ __forceinline__ void cis_decide(const NodeRec &nd, const Ray &R, floa
                 left_first = false;
                 return;
             }
+            if (order_resolve(nd, R, left_first)) return;
         }
     }
     float dl = FLT_MAX, dr = FLT_MAX;
@@ -315,8 +361,13 @@ __device__ __forceinline__ bool visit_leaf(const TriRec *tris, uint32_t n_tris, 
 // One lane = one ray at a time; each loop iteration visits one node.  Lanes
 // whose ray has finished take new rays from the global queue as soon as
 // kFetchIdle of them are idle, so warps stay full while the queue lasts.
+// blocks per SM the compiler must fit (0: no register cap)
+#ifndef RTA_TRACE_MIN_BLOCKS
+#define RTA_TRACE_MIN_BLOCKS 0
+#endif
+
 template <bool DIS, bool SHADOW, bool AILA, bool STATS, int STACK>
-__global__ void __launch_bounds__(kTraceThreads) k_trace(TraceArgs A)
+__global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(TraceArgs A)
 {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
