@@ -39,6 +39,8 @@ struct Ray {
     uint32_t zero;   // bit k: d[k] == 0
     float tmax;
     float rd[3];     // RN(1 / d[k]) for the slab filter
+    float ord[3];    // RN(o[k] * rd[k]): the filter's quotients are fma(plane, rd, -ord)
+    float eabs;      // absolute error term of those quotients, max |ord[k]| 2^-23 (+ 2^-146)
     bool fast;       // the slab filter applies (every nonzero |d[k]| in [2^-100, 2^100])
 };
 
@@ -56,6 +58,12 @@ __device__ __forceinline__ void make_ray(Ray &R, const float o[3], const float d
         R.rd[k] = d[k] == 0.0f ? 0.0f : __frcp_rn(d[k]);
     }
     R.tmax = tmax;
+    R.eabs = 1.12103877e-44f;   // 2^-146
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        R.ord[k] = __fmul_rn(o[k], R.rd[k]);
+        R.eabs = fmaxf(R.eabs, __fmaf_ru(fabsf(R.ord[k]), 1.19209290e-07f, 1.12103877e-44f));
+    }
 }
 
 // intersect_aabb (librta/intersect.h:56-150).  The reference walks the axes
@@ -97,13 +105,16 @@ __device__ __forceinline__ bool slab_test(float lx, float hx, float ly, float hy
 // The child-is step needs only decisions from the slab test: does each child
 // count as hit (inside, t_near <= t_far, t_far >= 0, and not culled:
 // t_near < best t, t_near <= t_max), and is the left t_near <= the right one.
-// With r = RN(1/d) and q = RN(a * r) each quotient is within |q| * 2^-22 of
-// RN(a / d) (two roundings of 2^-24 relative each against one), for normal
-// results; 2^-146 absolute covers subnormal ones.  t_near is a max and t_far
-// a min of such quotients, so the exact t_near / t_far lie within
-// |t| * 2^-21 + 2^-146 of the approximate ones (the bound of the quotient
-// that attains the max or min dominates every other's).  The bounds are
-// rounded outward.  A decision is taken from the intervals when it is the
+// With r = RN(1/d) and the fused quotient q = RN(plane * r - RN(o * r)) (one
+// FMA per plane), q is within |q| * 2^-21 + |o r| * 2^-23 of the reference's
+// RN(RN(plane - o) / d): relative roundings of 2^-24 for r, for o * r, for
+// the FMA, for plane - o and for the reference's division, plus the
+// cancellation term of o * r; 2^-146 absolute covers subnormal results.
+// t_near is a max and t_far a min of such quotients, so the exact t_near /
+// t_far lie within |t| * 2^-21 + max_k |o_k r_k| * 2^-23 + 2^-146 of the
+// approximate ones (the bound of the quotient that attains the max or min
+// dominates every other's; the absolute term is one per ray).  The bounds
+// are rounded outward.  A decision is taken from the intervals when it is the
 // same for every value in them; otherwise the step falls back to the exact
 // divisions.  NaN bounds (overflowing quotients) always count as uncertain.
 #ifndef RTA_SLAB_FILTER
@@ -125,15 +136,15 @@ __device__ __forceinline__ int slab_filter(float lx, float hx, float ly, float h
         if (R.zero & (1u << k)) {
             inside = inside && !(R.o[k] < bl[k] || R.o[k] > bh[k]);
         } else {
-            const float q1 = __fmul_rn(__fsub_rn(bl[k], R.o[k]), R.rd[k]);
-            const float q2 = __fmul_rn(__fsub_rn(bh[k], R.o[k]), R.rd[k]);
+            const float q1 = __fmaf_rn(bl[k], R.rd[k], -R.ord[k]);
+            const float q2 = __fmaf_rn(bh[k], R.rd[k], -R.ord[k]);
             tn = fmaxf(tn, fminf(q1, q2));
             tf = fminf(tf, fmaxf(q1, q2));
         }
     }
     if (!inside) return 0;
-    const float wn = __fmaf_ru(fabsf(tn), kFilterRel, kFilterAbs);
-    const float wf = __fmaf_ru(fabsf(tf), kFilterRel, kFilterAbs);
+    const float wn = __fmaf_ru(fabsf(tn), kFilterRel, R.eabs);
+    const float wf = __fmaf_ru(fabsf(tf), kFilterRel, R.eabs);
     const float tn_lo = __fsub_rd(tn, wn), tn_hi = __fadd_ru(tn, wn);
     const float tf_lo = __fsub_rd(tf, wf), tf_hi = __fadd_ru(tf, wf);
     // hit = t_near <= t_far && t_far >= 0; kept = hit && !(t_near >= best_t) && !(t_near > t_max)
