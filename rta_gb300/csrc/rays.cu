@@ -159,58 +159,66 @@ k_bounce(const TriRec *__restrict__ tris, const float *__restrict__ orig, const 
          uint32_t *__restrict__ osrc, uint32_t *__restrict__ tstat, FrameState *__restrict__ fs,
          uint32_t n_tris)
 {
-    __shared__ uint32_t s_tile, s_warp[kBounceThreads / 32], s_base;
+    constexpr int kWarps = kBounceThreads / 32;
+    constexpr int kChunks = kBounceItems * kWarps;   // 32-ray chunks of a tile, in ray order
+    static_assert(kChunks <= 32, "one warp scans the chunk counts");
+    __shared__ uint32_t s_tile, s_cnt[kChunks], s_base;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(&fs->tile_ctr, 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint32_t ntiles = (nrays + kBounceTile - 1) / kBounceTile;
-    // blocked arrangement: thread owns rays base + tid*ITEMS + k (ray order)
-    const uint32_t first = tile * kBounceTile + tid * kBounceItems;
+    // striped arrangement: item k of thread tid is ray tile*TILE + k*THREADS + tid,
+    // so every load of a warp is one contiguous run; chunk (k, w) = 32 rays in order
+    const uint32_t first = tile * kBounceTile + tid;
+    const uint32_t lt_mask = (1u << lane) - 1u;
     bool hit[kBounceItems];
-    uint32_t mine = 0;
+    uint32_t bal[kBounceItems];
 #pragma unroll
     for (int k = 0; k < kBounceItems; ++k) {
-        uint32_t i = first + k;
-        hit[k] = i < nrays && hits[i].t != FLT_MAX && hits[i].ref < n_tris;
-        mine += hit[k];
+        const uint32_t i = first + (uint32_t)k * kBounceThreads;
+        bool h = false;
+        if (i < nrays) {
+            const HitRec hr = hits[i];
+            h = hr.t != FLT_MAX && hr.ref < n_tris;
+        }
+        hit[k] = h;
+        bal[k] = __ballot_sync(0xffffffffu, h);
+        if (lane == 0) s_cnt[k * kWarps + w] = __popc(bal[k]);
     }
-    // block exclusive scan of per-thread counts
-    uint32_t x = mine;
+    __syncthreads();
+    if (w == 0) {
+        // exclusive scan of the chunk counts in ray order, then the tile's look-back
+        const uint32_t c = lane < kChunks ? s_cnt[lane] : 0u;
+        uint32_t x = c;
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
-        if (lane >= off) x += y;
-    }
-    if (lane == 31) s_warp[w] = x;
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t run = 0;
-        for (int j = 0; j < kBounceThreads / 32; ++j) {
-            uint32_t c = s_warp[j];
-            s_warp[j] = run;
-            run += c;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
         }
-        // run = tile total; publish and look back
-        uint32_t *my = tstat + tile;
-        uint32_t excl = 0;
-        if (tile == 0) {
-            st_volatile(my, kStatPrefix | run);
-        } else {
-            st_volatile(my, kStatAggregate | run);
-            excl = lookback(tstat, 1, tile, &fs->status);
-            __threadfence();
-            st_volatile(my, kStatPrefix | ((excl + run) & kStatValue));
+        if (lane < kChunks) s_cnt[lane] = x - c;
+        const uint32_t run = __shfl_sync(0xffffffffu, x, 31);
+        if (lane == 0) {
+            uint32_t *my = tstat + tile;
+            uint32_t excl = 0;
+            if (tile == 0) {
+                st_volatile(my, kStatPrefix | run);
+            } else {
+                st_volatile(my, kStatAggregate | run);
+                excl = lookback(tstat, 1, tile, &fs->status);
+                __threadfence();
+                st_volatile(my, kStatPrefix | ((excl + run) & kStatValue));
+            }
+            s_base = excl;
+            if (tile == ntiles - 1) fs->count = excl + run;
         }
-        s_base = excl;
-        if (tile == ntiles - 1) fs->count = excl + run;
     }
     __syncthreads();
-    uint32_t pos = s_base + s_warp[w] + x - mine;
 #pragma unroll
     for (int k = 0; k < kBounceItems; ++k) {
         if (!hit[k]) continue;
-        const uint32_t i = first + k;
+        const uint32_t i = first + (uint32_t)k * kBounceThreads;
+        const uint32_t pos = s_base + s_cnt[k * kWarps + w] + __popc(bal[k] & lt_mask);
         const HitRec hr = hits[i];
         const TriRec T = tris[hr.ref];
         V3 o = {orig[3 * (size_t)i], orig[3 * (size_t)i + 1], orig[3 * (size_t)i + 2]};
@@ -247,7 +255,6 @@ k_bounce(const TriRec *__restrict__ tris, const float *__restrict__ orig, const 
         oo[3 * (size_t)pos + 2] = __fadd_rn(p.z, __fmul_rn(nrm.z, eps));
         om[pos] = FLT_MAX;
         osrc[pos] = i;
-        ++pos;
     }
 }
 

@@ -503,10 +503,20 @@ __global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(T
             bool pop = false;
             if (!is_leaf(cur)) {
                 ++inner_visits;
-                float dist = FLT_MAX;
-                bool h = AILA ? aila_test(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], R.o, id, best.t, dist)
-                              : slab_test(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], R, dist);
-                if (dist >= best.t || dist > R.tmax) h = false;
+                bool h;
+                int certain = 2;
+                if (!AILA && RTA_SLAB_FILTER && R.fast) {
+                    float lo, hi;
+                    certain = slab_filter(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], R, best.t, lo, hi);
+                }
+                if (certain != 2) {
+                    h = certain == 1;
+                } else {
+                    float dist = FLT_MAX;
+                    h = AILA ? aila_test(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], R.o, id, best.t, dist)
+                             : slab_test(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], R, dist);
+                    if (dist >= best.t || dist > R.tmax) h = false;
+                }
                 if (h) {
                     if (sp + 1 >= STACK) {
                         overflow = true;
