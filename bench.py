@@ -704,7 +704,9 @@ def run_gb300(args):
                 "how": "one rta_host_frames_run per step on pinned host buffers: rays copied in, frame, "
                        "primary + bounce hits and bounce count copied out; copies on their own streams "
                        "overlap the neighbouring steps' traversal"},
-        "gpu_launches": 5 * args.steps,
+        # per timed frame: the fused trace (primary + bounce rays) and the
+        # bounce gather (the L2 flush between frames is a torch fill)
+        "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
         "build": {"ms": bmean, "ms_min": min(build_ms), "mtri_s": n / (bmean * 1e-3) / 1e6,
                   "algorithmic_bytes": 372 * n, "achieved_gbs": 372 * n / (bmean * 1e-3) / 1e9,

@@ -10,44 +10,16 @@
 #include <cstring>
 #include <mutex>
 
-#include "common.cuh"
+#include "bounce.cuh"
 
 namespace rta {
 
 int trace_impl(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt,
                uint32_t nrays, const uint32_t *d_nrays, void *hits, uint32_t mode, uint32_t *stats,
                uint32_t *queue, cudaStream_t s);
-
-// librta/cuda-vec.h:157-193 in the same operation order
-struct V3 {
-    float x, y, z;
-};
-__device__ __forceinline__ V3 v_div(V3 a, float s)
-{
-    return {__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s)};
-}
-__device__ __forceinline__ V3 v_mul(V3 a, float s)
-{
-    return {__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s)};
-}
-__device__ __forceinline__ V3 v_add(V3 a, V3 b)
-{
-    return {__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)};
-}
-__device__ __forceinline__ float v_dot(V3 a, V3 b)
-{
-    float s = __fmul_rn(a.x, b.x);
-    s = __fadd_rn(s, __fmul_rn(a.y, b.y));
-    s = __fadd_rn(s, __fmul_rn(a.z, b.z));
-    return s;
-}
-__device__ __forceinline__ float v_len(V3 a) { return __fsqrt_rn(v_dot(a, a)); }
-__device__ __forceinline__ V3 v_cross(V3 l, V3 r)
-{
-    return {__fsub_rn(__fmul_rn(l.y, r.z), __fmul_rn(l.z, r.y)),
-            __fsub_rn(__fmul_rn(l.z, r.x), __fmul_rn(l.x, r.z)),
-            __fsub_rn(__fmul_rn(l.x, r.y), __fmul_rn(l.y, r.x))};
-}
+int trace_frame_fused(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt, uint32_t nrays,
+                      void *hits, uint32_t seed, float eps, float *b_orig, float *b_dir, void *b_hits,
+                      uint32_t *b_flag, uint32_t *queue, cudaStream_t s);
 
 __global__ void k_shirley(float *__restrict__ dirs, float *__restrict__ orgs, float *__restrict__ maxts,
                           float height, float aspect, int w, int h, V3 vd, V3 pos, V3 up, float maxt)
@@ -90,56 +62,6 @@ __global__ void k_reset(HitRec *__restrict__ hits, uint32_t n, const uint32_t *_
 }
 
 // ---- diffuse bounce ---- //
-
-// 32-bit xor-shift-multiply finaliser; the oracle uses the same function
-__device__ __forceinline__ uint32_t hash32(uint32_t x)
-{
-    x ^= x >> 16;
-    x *= 0x7feb352du;
-    x ^= x >> 15;
-    x *= 0x846ca68bu;
-    x ^= x >> 16;
-    return x;
-}
-
-__device__ __forceinline__ float uniform01(uint32_t seed, uint32_t index)
-{
-    uint32_t h = hash32(index * 0x9e3779b1u + hash32(seed ^ 0x5bd1e995u));
-    return __fmul_rn((float)(h >> 8), 1.0f / 16777216.0f);
-}
-
-// cos and sin of 2*pi*u: quarter-turn reduction and Taylor polynomials in
-// Horner form with fused multiply-adds -- IEEE operations only, so the
-// oracle reproduces them bit for bit
-__device__ __forceinline__ void cos_sin_2pi(float u, float &c, float &s)
-{
-    float u4 = __fmul_rn(u, 4.0f);
-    int q = (int)u4;
-    if (q > 3) q = 3;
-    float f = __fsub_rn(u4, (float)q);
-    float th = __fmul_rn(f, 1.57079637f);
-    float x2 = __fmul_rn(th, th);
-    float sp = -2.50521084e-08f;
-    sp = __fmaf_rn(sp, x2, 2.75573192e-06f);
-    sp = __fmaf_rn(sp, x2, -1.98412698e-04f);
-    sp = __fmaf_rn(sp, x2, 8.33333333e-03f);
-    sp = __fmaf_rn(sp, x2, -1.66666667e-01f);
-    sp = __fmaf_rn(sp, x2, 1.0f);
-    float sn = __fmul_rn(sp, th);
-    float cp = 2.08767570e-09f;
-    cp = __fmaf_rn(cp, x2, -2.75573192e-07f);
-    cp = __fmaf_rn(cp, x2, 2.48015873e-05f);
-    cp = __fmaf_rn(cp, x2, -1.38888889e-03f);
-    cp = __fmaf_rn(cp, x2, 4.16666667e-02f);
-    cp = __fmaf_rn(cp, x2, -0.5f);
-    float cs = __fmaf_rn(cp, x2, 1.0f);
-    switch (q) {
-    case 0: c = cs; s = sn; break;
-    case 1: c = -sn; s = cs; break;
-    case 2: c = -cs; s = -sn; break;
-    default: c = sn; s = -cs; break;
-    }
-}
 
 constexpr int kBounceThreads = 256;
 constexpr int kBounceItems = 4;
@@ -220,39 +142,16 @@ k_bounce(const TriRec *__restrict__ tris, const float *__restrict__ orig, const 
         const uint32_t i = first + (uint32_t)k * kBounceThreads;
         const uint32_t pos = s_base + s_cnt[k * kWarps + w] + __popc(bal[k] & lt_mask);
         const HitRec hr = hits[i];
-        const TriRec T = tris[hr.ref];
-        V3 o = {orig[3 * (size_t)i], orig[3 * (size_t)i + 1], orig[3 * (size_t)i + 2]};
-        V3 d = {dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]};
-        V3 p = {__fadd_rn(o.x, __fmul_rn(hr.t, d.x)), __fadd_rn(o.y, __fmul_rn(hr.t, d.y)),
-                __fadd_rn(o.z, __fmul_rn(hr.t, d.z))};
-        V3 e1 = {__fsub_rn(T.v1.x, T.v0.x), __fsub_rn(T.v1.y, T.v0.y), __fsub_rn(T.v1.z, T.v0.z)};
-        V3 e2 = {__fsub_rn(T.v2.x, T.v0.x), __fsub_rn(T.v2.y, T.v0.y), __fsub_rn(T.v2.z, T.v0.z)};
-        V3 nrm = v_cross(e1, e2);
-        nrm = v_div(nrm, v_len(nrm));
-        if (v_dot(nrm, d) > 0.0f) nrm = {-nrm.x, -nrm.y, -nrm.z};
-        const float u1 = uniform01(seed, 2u * i), u2 = uniform01(seed, 2u * i + 1u);
-        const float rr = __fsqrt_rn(u1);
-        float cs, sn;
-        cos_sin_2pi(u2, cs, sn);
-        const float lx = __fmul_rn(rr, cs), ly = __fmul_rn(rr, sn);
-        const float one_m = __fsub_rn(1.0f, u1);
-        const float lz = __fsqrt_rn(one_m > 0.0f ? one_m : 0.0f);
-        // orthonormal basis: Duff et al., JCGT 6(1), 2017
-        const float sg = copysignf(1.0f, nrm.z);
-        const float a = __fdiv_rn(-1.0f, __fadd_rn(sg, nrm.z));
-        const float b = __fmul_rn(__fmul_rn(nrm.x, nrm.y), a);
-        const V3 b1 = {__fadd_rn(1.0f, __fmul_rn(__fmul_rn(__fmul_rn(sg, nrm.x), nrm.x), a)),
-                       __fmul_rn(sg, b), -__fmul_rn(sg, nrm.x)};
-        const V3 b2 = {b, __fadd_rn(sg, __fmul_rn(__fmul_rn(nrm.y, nrm.y), a)), -nrm.y};
-        const float bx = __fadd_rn(__fadd_rn(__fmul_rn(b1.x, lx), __fmul_rn(b2.x, ly)), __fmul_rn(nrm.x, lz));
-        const float by = __fadd_rn(__fadd_rn(__fmul_rn(b1.y, lx), __fmul_rn(b2.y, ly)), __fmul_rn(nrm.y, lz));
-        const float bz = __fadd_rn(__fadd_rn(__fmul_rn(b1.z, lx), __fmul_rn(b2.z, ly)), __fmul_rn(nrm.z, lz));
-        od[3 * (size_t)pos + 0] = bx;
-        od[3 * (size_t)pos + 1] = by;
-        od[3 * (size_t)pos + 2] = bz;
-        oo[3 * (size_t)pos + 0] = __fadd_rn(p.x, __fmul_rn(nrm.x, eps));
-        oo[3 * (size_t)pos + 1] = __fadd_rn(p.y, __fmul_rn(nrm.y, eps));
-        oo[3 * (size_t)pos + 2] = __fadd_rn(p.z, __fmul_rn(nrm.z, eps));
+        const float o[3] = {orig[3 * (size_t)i], orig[3 * (size_t)i + 1], orig[3 * (size_t)i + 2]};
+        const float d[3] = {dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]};
+        float bo[3], bd[3];
+        bounce_ray(tris[hr.ref], o, d, hr.t, i, seed, eps, bo, bd);
+        od[3 * (size_t)pos + 0] = bd[0];
+        od[3 * (size_t)pos + 1] = bd[1];
+        od[3 * (size_t)pos + 2] = bd[2];
+        oo[3 * (size_t)pos + 0] = bo[0];
+        oo[3 * (size_t)pos + 1] = bo[1];
+        oo[3 * (size_t)pos + 2] = bo[2];
         om[pos] = FLT_MAX;
         osrc[pos] = i;
     }
@@ -262,6 +161,78 @@ k_bounce(const TriRec *__restrict__ tris, const float *__restrict__ orig, const 
 
 using namespace rta;
 
+// The fused frame's bounce rays and hits, gathered from the per-primary-ray
+// slots into the frame's buffers in primary-ray order (bounce ray k = the k-th
+// flagged ray), with the same single-pass ordered scan as k_bounce.
+__global__ void __launch_bounds__(kBounceThreads)
+k_bounce_gather(const uint32_t *__restrict__ flag, const float *__restrict__ s_orig,
+                const float *__restrict__ s_dir, const HitRec *__restrict__ s_hits, uint32_t nrays,
+                float *__restrict__ oo, float *__restrict__ od, float *__restrict__ om, uint32_t *__restrict__ osrc,
+                HitRec *__restrict__ ohits, uint32_t *__restrict__ tstat, FrameState *__restrict__ fs)
+{
+    constexpr int kWarps = kBounceThreads / 32;
+    constexpr int kChunks = kBounceItems * kWarps;
+    __shared__ uint32_t s_tile, s_cnt[kChunks], s_base;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(&fs->tile_ctr, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t ntiles = (nrays + kBounceTile - 1) / kBounceTile;
+    const uint32_t first = tile * kBounceTile + tid;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    bool hit[kBounceItems];
+    uint32_t bal[kBounceItems];
+#pragma unroll
+    for (int k = 0; k < kBounceItems; ++k) {
+        const uint32_t i = first + (uint32_t)k * kBounceThreads;
+        hit[k] = i < nrays && flag[i] != 0u;
+        bal[k] = __ballot_sync(0xffffffffu, hit[k]);
+        if (lane == 0) s_cnt[k * kWarps + w] = __popc(bal[k]);
+    }
+    __syncthreads();
+    if (w == 0) {
+        const uint32_t c = lane < kChunks ? s_cnt[lane] : 0u;
+        uint32_t x = c;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane < kChunks) s_cnt[lane] = x - c;
+        const uint32_t run = __shfl_sync(0xffffffffu, x, 31);
+        if (lane == 0) {
+            uint32_t *my = tstat + tile;
+            uint32_t excl = 0;
+            if (tile == 0) {
+                st_volatile(my, kStatPrefix | run);
+            } else {
+                st_volatile(my, kStatAggregate | run);
+                excl = lookback(tstat, 1, tile, &fs->status);
+                __threadfence();
+                st_volatile(my, kStatPrefix | ((excl + run) & kStatValue));
+            }
+            s_base = excl;
+            if (tile == ntiles - 1) fs->count = excl + run;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kBounceItems; ++k) {
+        if (!hit[k]) continue;
+        const uint32_t i = first + (uint32_t)k * kBounceThreads;
+        const uint32_t pos = s_base + s_cnt[k * kWarps + w] + __popc(bal[k] & lt_mask);
+        oo[3 * (size_t)pos + 0] = s_orig[3 * (size_t)i + 0];
+        oo[3 * (size_t)pos + 1] = s_orig[3 * (size_t)i + 1];
+        oo[3 * (size_t)pos + 2] = s_orig[3 * (size_t)i + 2];
+        od[3 * (size_t)pos + 0] = s_dir[3 * (size_t)i + 0];
+        od[3 * (size_t)pos + 1] = s_dir[3 * (size_t)i + 1];
+        od[3 * (size_t)pos + 2] = s_dir[3 * (size_t)i + 2];
+        om[pos] = FLT_MAX;
+        osrc[pos] = i;
+        ohits[pos] = s_hits[i];
+    }
+}
+
 struct rta_frame_ctx {
     uint32_t cap = 0;
     float *orig = nullptr, *dir = nullptr, *maxt = nullptr;
@@ -269,6 +240,10 @@ struct rta_frame_ctx {
     HitRec *hits = nullptr;
     uint32_t *tstat = nullptr;
     FrameState *fs = nullptr;
+    // per-primary-ray slots of the fused frame: bounce ray, its hit, a flag
+    float *s_orig = nullptr, *s_dir = nullptr;
+    HitRec *s_hits = nullptr;
+    uint32_t *s_flag = nullptr;
 };
 
 extern "C" {
@@ -309,6 +284,10 @@ int rta_frame_create(rta_frame_ctx **out, uint32_t max_rays)
     e = e ? e : cudaMalloc(&c->hits, (size_t)max_rays * sizeof(HitRec));
     e = e ? e : cudaMalloc(&c->tstat, (size_t)tiles * 4);
     e = e ? e : cudaMalloc(&c->fs, sizeof(FrameState));
+    e = e ? e : cudaMalloc(&c->s_orig, (size_t)max_rays * 12);
+    e = e ? e : cudaMalloc(&c->s_dir, (size_t)max_rays * 12);
+    e = e ? e : cudaMalloc(&c->s_hits, (size_t)max_rays * sizeof(HitRec));
+    e = e ? e : cudaMalloc(&c->s_flag, (size_t)max_rays * 4);
     e = e ? e : cudaMemset(c->fs, 0, sizeof(FrameState));
     if (e != cudaSuccess) {
         set_cuda_error(e, "rta_frame_create");
@@ -322,7 +301,8 @@ int rta_frame_create(rta_frame_ctx **out, uint32_t max_rays)
 int rta_frame_destroy(rta_frame_ctx *c)
 {
     if (!c) return RTA_ERR_INVALID;
-    void *ptrs[] = {c->orig, c->dir, c->maxt, c->src, c->hits, c->tstat, c->fs};
+    void *ptrs[] = {c->orig, c->dir, c->maxt, c->src, c->hits, c->tstat, c->fs,
+                    c->s_orig, c->s_dir, c->s_hits, c->s_flag};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -365,6 +345,19 @@ int rta_frame_run(rta_frame_ctx *c, const rta_lbvh *bvh, const float *orig, cons
         return RTA_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t mode_nostats = mode & ~RTA_TRACE_STATS;
+    if (mode_nostats == RTA_TRACE_CIS) {
+        // one launch traces every primary ray and, right after it, its bounce
+        // ray; a gather then lays the bounce rays and hits out in primary order
+        int rc = trace_frame_fused(bvh, orig, dir, maxt, nrays, hits, seed, eps, c->s_orig, c->s_dir, c->s_hits,
+                                   c->s_flag, &c->fs->queue, s);
+        if (rc) return rc;
+        const uint32_t tiles = (nrays + kBounceTile - 1) / kBounceTile;
+        RTA_CUDA_TRY(cudaMemsetAsync(c->tstat, 0, (size_t)tiles * 4, s));
+        RTA_CUDA_TRY(cudaMemsetAsync(&c->fs->tile_ctr, 0, 4, s));
+        k_bounce_gather<<<tiles, kBounceThreads, 0, s>>>(c->s_flag, c->s_orig, c->s_dir, c->s_hits, nrays, c->orig,
+                                                         c->dir, c->maxt, c->src, c->hits, c->tstat, c->fs);
+        return check_launch("k_bounce_gather");
+    }
     const uint32_t rb = (nrays + 255) / 256 < 4096 ? (nrays + 255) / 256 : 4096;
     k_reset<<<rb, 256, 0, s>>>((HitRec *)hits, nrays, nullptr);
     int rc = check_launch("k_reset");

@@ -14,6 +14,7 @@
 // so hits, including which of two equal-t triangles wins, are the reference's.
 #include "common.cuh"
 #include "batch.cuh"
+#include "bounce.cuh"
 #include "mlp.cuh"
 
 namespace rta {
@@ -30,6 +31,14 @@ struct TraceArgs {
     uint32_t *queue;    // ray batch counter, zero at launch
     uint32_t *status;
     uint32_t n_tris;    // bounds every link and triangle index before use
+    // FUSE (frame with one diffuse bounce): each primary hit's bounce ray is
+    // traced by the same lane right after it; its ray and hit go to the
+    // primary ray's slot, flagged, for the ordered compaction that follows
+    uint32_t seed;
+    float eps;
+    float *b_orig, *b_dir;
+    HitRec *b_hits;
+    uint32_t *b_flag;
 };
 
 // Per-ray constants of the slab test: the ray and which direction components
@@ -377,9 +386,10 @@ __device__ __forceinline__ bool visit_leaf(const TriRec *tris, uint32_t n_tris, 
 #define RTA_TRACE_MIN_BLOCKS 0
 #endif
 
-template <bool DIS, bool SHADOW, bool AILA, bool STATS, int STACK>
+template <bool DIS, bool SHADOW, bool AILA, bool STATS, int STACK, bool FUSE = false>
 __global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(TraceArgs A)
 {
+    static_assert(!FUSE || (!DIS && !SHADOW && !AILA && !STATS), "the fused frame is child-is closest hit");
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
     const uint32_t nrays = A.d_nrays ? *A.d_nrays : A.nrays;
@@ -395,6 +405,7 @@ __global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(T
     Best best;
     float bx[6];   // DIS: box of the current node
     bool overflow = false, capped = false, bad = false;
+    bool second = false;   // FUSE: the lane traces ray r's bounce ray
 
     for (;;) {
         const uint32_t idle = __ballot_sync(0xffffffffu, !active);
@@ -432,6 +443,7 @@ __global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(T
                         bx[0] = root.lo[0]; bx[1] = root.hi[0]; bx[2] = root.lo[1];
                         bx[3] = root.hi[1]; bx[4] = root.lo[2]; bx[5] = root.hi[2];
                     }
+                    second = false;
                     active = true;
                 }
             }
@@ -564,17 +576,54 @@ __global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(T
             }
         }
         if (done) {
-            if (best.t != FLT_MAX) {
-                reinterpret_cast<float4 *>(A.hits)[r] =
-                    make_float4(best.t, best.beta, best.gamma, __uint_as_float(best.ref));
+            if (FUSE) {
+                // a miss leaves the record as the frame's reset left it:
+                // t = FLT_MAX, beta = 1, gamma = 2 (reset_intersections), ref kept
+                HitRec *out = second ? A.b_hits : A.hits;
+                if (best.t != FLT_MAX) {
+                    reinterpret_cast<float4 *>(out)[r] =
+                        make_float4(best.t, best.beta, best.gamma, __uint_as_float(best.ref));
+                } else {
+                    out[r].t = FLT_MAX;
+                    out[r].beta = 1.0f;
+                    out[r].gamma = 2.0f;
+                }
+                const bool bounce = !second && best.t != FLT_MAX && best.ref < A.n_tris;
+                if (!second) A.b_flag[r] = bounce ? 1u : 0u;
+                if (bounce) {
+                    // the bounce ray of this hit (bounce.cuh), traced next by this lane
+                    float bo[3], bd[3];
+                    bounce_ray(load_tri(A.tris, best.ref), R.o, R.d, best.t, r, A.seed, A.eps, bo, bd);
+                    A.b_orig[3 * (size_t)r + 0] = bo[0];
+                    A.b_orig[3 * (size_t)r + 1] = bo[1];
+                    A.b_orig[3 * (size_t)r + 2] = bo[2];
+                    A.b_dir[3 * (size_t)r + 0] = bd[0];
+                    A.b_dir[3 * (size_t)r + 1] = bd[1];
+                    A.b_dir[3 * (size_t)r + 2] = bd[2];
+                    make_ray(R, bo, bd, FLT_MAX);
+                    best.t = FLT_MAX;
+                    best.beta = best.gamma = 0.f;
+                    best.ref = 0;
+                    sp = -1;
+                    steps = 0;
+                    cur = root.link;
+                    second = true;
+                } else {
+                    active = false;
+                }
             } else {
-                A.hits[r].t = FLT_MAX;
+                if (best.t != FLT_MAX) {
+                    reinterpret_cast<float4 *>(A.hits)[r] =
+                        make_float4(best.t, best.beta, best.gamma, __uint_as_float(best.ref));
+                } else {
+                    A.hits[r].t = FLT_MAX;
+                }
+                if (STATS) {
+                    A.stats[2 * (size_t)r + 0] = inner_visits;
+                    A.stats[2 * (size_t)r + 1] = tri_tests;
+                }
+                active = false;
             }
-            if (STATS) {
-                A.stats[2 * (size_t)r + 0] = inner_visits;
-                A.stats[2 * (size_t)r + 1] = tri_tests;
-            }
-            active = false;
         }
     }
     if (overflow) atomicOr(A.status, RTA_DEV_STACK_OVERFLOW);
@@ -1100,6 +1149,52 @@ static int launch_trace(const TraceArgs &a, cudaStream_t s)
     }
     k_trace<DIS, SHADOW, AILA, STATS, STACK><<<blocks, kTraceThreads, 0, s>>>(a);
     return check_launch("k_trace");
+}
+
+// The frame's primary pass with each bounce ray traced right after its
+// primary ray (child-is closest hit).  b_* are per-primary-ray slots.
+template <int STACK>
+static int launch_fused(const TraceArgs &a, cudaStream_t s)
+{
+    static int blocks = 0;
+    if (!blocks) {
+        int per_sm = 0, dev = 0, sms = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false, false, false, false, STACK, true>,
+                                                      kTraceThreads, 0);
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    }
+    k_trace<false, false, false, false, STACK, true><<<blocks, kTraceThreads, 0, s>>>(a);
+    return check_launch("k_trace fused frame");
+}
+
+int trace_frame_fused(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt, uint32_t nrays,
+                      void *hits, uint32_t seed, float eps, float *b_orig, float *b_dir, void *b_hits,
+                      uint32_t *b_flag, uint32_t *queue, cudaStream_t s)
+{
+    TraceArgs a;
+    a.nodes = (const NodeRec *)bvh->nodes;
+    a.root = (const RootRec *)bvh->root;
+    a.tris = (const TriRec *)bvh->tris;
+    a.orig = orig;
+    a.dir = dir;
+    a.maxt = maxt;
+    a.nrays = nrays;
+    a.d_nrays = nullptr;
+    a.hits = (HitRec *)hits;
+    a.stats = nullptr;
+    a.queue = queue;
+    a.status = bvh->status;
+    a.n_tris = bvh->n;
+    a.seed = seed;
+    a.eps = eps;
+    a.b_orig = b_orig;
+    a.b_dir = b_dir;
+    a.b_hits = (HitRec *)b_hits;
+    a.b_flag = b_flag;
+    RTA_CUDA_TRY(cudaMemsetAsync(queue, 0, 4, s));
+    return bvh->morton_bits == 63 ? launch_fused<80>(a, s) : launch_fused<40>(a, s);
 }
 
 template <int STACK>
