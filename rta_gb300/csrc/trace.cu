@@ -381,6 +381,12 @@ __device__ __forceinline__ bool visit_leaf(const TriRec *tris, uint32_t n_tris, 
 // One lane = one ray at a time; each loop iteration visits one node.  Lanes
 // whose ray has finished take new rays from the global queue as soon as
 // kFetchIdle of them are idle, so warps stay full while the queue lasts.
+// a lane at a leaf waits for this many leaf lanes before testing (0: never
+// waits); 4 measured best on the 1080p terrain frame (2 %, sweep 2-16)
+#ifndef RTA_LEAF_PARK
+#define RTA_LEAF_PARK 4
+#endif
+
 // blocks per SM the compiler must fit (0: no register cap)
 #ifndef RTA_TRACE_MIN_BLOCKS
 #define RTA_TRACE_MIN_BLOCKS 0
@@ -451,6 +457,16 @@ __global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(T
         if (!__any_sync(0xffffffffu, active)) {
             if (exhausted) break;
             continue;
+        }
+        if (!DIS && RTA_LEAF_PARK > 0) {
+            // a lane at a leaf waits until enough lanes of the warp are at
+            // leaves (or every active lane is), so the warp runs the triangle
+            // tests together instead of beside inner-node steps; each ray
+            // still visits its nodes in the same order
+            const bool at_leaf = active && is_leaf(cur);
+            const uint32_t lm = __ballot_sync(0xffffffffu, at_leaf);
+            const uint32_t am = __ballot_sync(0xffffffffu, active);
+            if (at_leaf && __popc(lm) < RTA_LEAF_PARK && lm != am) continue;
         }
         if (!active) continue;
 
