@@ -715,6 +715,12 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_batch(BatchTraceArgs A)
             if (exhausted) break;
             continue;
         }
+        if (RTA_LEAF_PARK > 0) {   // leaf parking as in k_trace
+            const bool at_leaf = active && is_leaf(cur);
+            const uint32_t lm = __ballot_sync(0xffffffffu, at_leaf);
+            const uint32_t am = __ballot_sync(0xffffffffu, active);
+            if (at_leaf && __popc(lm) < RTA_LEAF_PARK && lm != am) continue;
+        }
         if (!active) continue;
 
         bool done = false;
