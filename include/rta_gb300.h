@@ -186,6 +186,15 @@ int rta_frame_run(rta_frame_ctx *ctx, const rta_lbvh *bvh, const float *orig, co
 /* Synchronises and returns the frame's device status flags. */
 int rta_frame_status(rta_frame_ctx *ctx, rta_stream_t stream, uint32_t *flags);
 
+/* Per-pass timing, as basic_raytracer::timings records it (librta/raytrav.h:
+ * 426): with timing on, rta_frame_run records CUDA events on its stream around
+ * the frame's trace work (the fused trace launch of a child-is frame; primary
+ * trace to bounce trace otherwise; the bounce gather is not included), and
+ * rta_frame_trace_ms waits for the last run's end event and returns the
+ * milliseconds between them.  Invalid before a timed run. */
+int rta_frame_set_timing(rta_frame_ctx *ctx, int on);
+int rta_frame_trace_ms(rta_frame_ctx *ctx, float *ms);
+
 /* Frames on host buffers (no counterpart in the reference, whose frames
  * start and end in device memory; its driver downloads the hits, see
  * primary_intersection_downloader, librta/cuda.h:222-245).  Each run copies

@@ -244,6 +244,9 @@ struct rta_frame_ctx {
     float *s_orig = nullptr, *s_dir = nullptr;
     HitRec *s_hits = nullptr;
     uint32_t *s_flag = nullptr;
+    // optional events around the frame's trace work (rta_frame_set_timing)
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    bool timing = false, timed = false;
 };
 
 extern "C" {
@@ -301,6 +304,8 @@ int rta_frame_create(rta_frame_ctx **out, uint32_t max_rays)
 int rta_frame_destroy(rta_frame_ctx *c)
 {
     if (!c) return RTA_ERR_INVALID;
+    if (c->ev_begin) cudaEventDestroy(c->ev_begin);
+    if (c->ev_end) cudaEventDestroy(c->ev_end);
     void *ptrs[] = {c->orig, c->dir, c->maxt, c->src, c->hits, c->tstat, c->fs,
                     c->s_orig, c->s_dir, c->s_hits, c->s_flag};
     for (void *p : ptrs)
@@ -345,12 +350,17 @@ int rta_frame_run(rta_frame_ctx *c, const rta_lbvh *bvh, const float *orig, cons
         return RTA_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t mode_nostats = mode & ~RTA_TRACE_STATS;
+    if (c->timing) RTA_CUDA_TRY(cudaEventRecord(c->ev_begin, s));
     if (mode_nostats == RTA_TRACE_CIS) {
         // one launch traces every primary ray and, right after it, its bounce
         // ray; a gather then lays the bounce rays and hits out in primary order
         int rc = trace_frame_fused(bvh, orig, dir, maxt, nrays, hits, seed, eps, c->s_orig, c->s_dir, c->s_hits,
                                    c->s_flag, &c->fs->queue, s);
         if (rc) return rc;
+        if (c->timing) {
+            RTA_CUDA_TRY(cudaEventRecord(c->ev_end, s));
+            c->timed = true;
+        }
         const uint32_t tiles = (nrays + kBounceTile - 1) / kBounceTile;
         RTA_CUDA_TRY(cudaMemsetAsync(c->tstat, 0, (size_t)tiles * 4, s));
         RTA_CUDA_TRY(cudaMemsetAsync(&c->fs->tile_ctr, 0, 4, s));
@@ -368,8 +378,34 @@ int rta_frame_run(rta_frame_ctx *c, const rta_lbvh *bvh, const float *orig, cons
     if (rc) return rc;
     k_reset<<<rb, 256, 0, s>>>(c->hits, nrays, &c->fs->count);
     if ((rc = check_launch("k_reset"))) return rc;
-    return trace_impl(bvh, c->orig, c->dir, c->maxt, nrays, &c->fs->count, c->hits, mode_nostats,
-                      nullptr, &c->fs->queue, s);
+    rc = trace_impl(bvh, c->orig, c->dir, c->maxt, nrays, &c->fs->count, c->hits, mode_nostats, nullptr,
+                    &c->fs->queue, s);
+    if (rc) return rc;
+    if (c->timing) {
+        RTA_CUDA_TRY(cudaEventRecord(c->ev_end, s));
+        c->timed = true;
+    }
+    return RTA_OK;
+}
+
+int rta_frame_set_timing(rta_frame_ctx *c, int on)
+{
+    if (!c) return RTA_ERR_INVALID;
+    if (on && !c->ev_begin) {
+        RTA_CUDA_TRY(cudaEventCreate(&c->ev_begin));
+        RTA_CUDA_TRY(cudaEventCreate(&c->ev_end));
+    }
+    c->timing = on != 0;
+    c->timed = false;
+    return RTA_OK;
+}
+
+int rta_frame_trace_ms(rta_frame_ctx *c, float *ms)
+{
+    if (!c || !ms || !c->timed) return RTA_ERR_INVALID;
+    RTA_CUDA_TRY(cudaEventSynchronize(c->ev_end));
+    RTA_CUDA_TRY(cudaEventElapsedTime(ms, c->ev_begin, c->ev_end));
+    return RTA_OK;
 }
 
 int rta_frame_status(rta_frame_ctx *c, rta_stream_t stream, uint32_t *flags)

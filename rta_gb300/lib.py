@@ -24,7 +24,7 @@ SYMBOLS = [
     "rta_lbvh_reserve", "rta_lbvh_set_digit_bits", "rta_lbvh_build", "rta_lbvh_get", "rta_lbvh_status", "rta_lbvh_to_2f4",
     "rta_trace", "rta_setup_shirley_rays", "rta_reset_intersections", "rta_frame_create",
     "rta_frame_destroy", "rta_frame_get", "rta_diffuse_bounce", "rta_frame_run",
-    "rta_frame_status", "rta_host_frames_create", "rta_host_frames_destroy", "rta_host_frames_run",
+    "rta_frame_status", "rta_frame_set_timing", "rta_frame_trace_ms", "rta_host_frames_create", "rta_host_frames_destroy", "rta_host_frames_run",
     "rta_diffuse_bounce_noalloc", "rta_order_create", "rta_order_destroy",
     "rta_order_param_count", "rta_order_get_params", "rta_order_set_params", "rta_order_sample",
     "rta_order_sample_count", "rta_order_clear_samples", "rta_order_samples", "rta_order_gradient",
@@ -96,6 +96,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_diffuse_bounce.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, u32, f32, vp]
     L.rta_frame_run.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, vp, u32, u32, f32, vp]
     L.rta_frame_status.argtypes = [vp, vp, P(u32)]
+    L.rta_frame_set_timing.argtypes = [vp, i32]
+    L.rta_frame_trace_ms.argtypes = [vp, P(f32)]
     L.rta_host_frames_create.argtypes = [P(vp), u32]
     L.rta_host_frames_destroy.argtypes = [vp]
     L.rta_host_frames_run.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, vp, vp, vp, u32, u32, f32, vp]

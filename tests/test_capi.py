@@ -54,6 +54,9 @@ def test_invalid_arguments_are_rejected_without_a_device(lib):
             assert lib.rta_lbvh_set_digit_bits(h, bad) == L.ERR_INVALID
         for good in (8, 10, 11):
             assert lib.rta_lbvh_set_digit_bits(h, good) == L.OK
+        ms = C.c_float(0)
+        assert lib.rta_frame_set_timing(None, 1) == L.ERR_INVALID
+        assert lib.rta_frame_trace_ms(None, C.byref(ms)) == L.ERR_INVALID
     finally:
         assert lib.rta_lbvh_destroy(h) == L.OK
     assert lib.rta_trace(None, None, None, None, 0, None, None, 0, None, None) == L.ERR_INVALID

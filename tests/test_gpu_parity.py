@@ -468,3 +468,35 @@ def test_host_frames_pipeline_matches_device_frames():
         for fld in ("beta", "gamma", "ref"):
             np.testing.assert_array_equal(got_b[fld][v].view(np.uint32), want_b[fld][v].view(np.uint32))
         lib.rta_frame_destroy(fh)
+
+
+def test_frame_trace_timing():
+    """rta_frame_set_timing / rta_frame_trace_ms: invalid before a timed run,
+    then the trace time of the last frame, below the whole frame's time."""
+    import ctypes as C
+    tris = S.terrain(128, 64, seed=5)
+    cam = S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), w=320, h=180)
+    n = cam.w * cam.h
+    o, d, m = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
+    dev = torch.device("cuda")
+    do, dd, dm = (torch.from_numpy(np.ascontiguousarray(x, np.float32).reshape(-1)).to(dev) for x in (o, d, m))
+    hh = torch.zeros(4 * n, dtype=torch.float32, device=dev)
+    bvh = gpu_build(tris, 30)
+    lib = L.load()
+    fh = C.c_void_p()
+    L.check(lib.rta_frame_create(C.byref(fh), n), "rta_frame_create")
+    try:
+        ms = C.c_float(0)
+        assert lib.rta_frame_trace_ms(fh, C.byref(ms)) == L.ERR_INVALID
+        L.check(lib.rta_frame_set_timing(fh, 1), "rta_frame_set_timing")
+        for mode in (L.TRACE_CIS, L.TRACE_DIS):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            L.check(lib.rta_frame_run(fh, C.byref(bvh.view), P._ptr(do), P._ptr(dd), P._ptr(dm), n, P._ptr(hh),
+                                      mode, 3, np.float32(1e-4), P._stream()), "rta_frame_run")
+            e1.record()
+            e1.synchronize()
+            L.check(lib.rta_frame_trace_ms(fh, C.byref(ms)), "rta_frame_trace_ms")
+            assert 0.0 < ms.value <= e0.elapsed_time(e1) * 1.05 + 0.01
+    finally:
+        lib.rta_frame_destroy(fh)
