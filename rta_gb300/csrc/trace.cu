@@ -691,7 +691,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_batch(BatchTraceArgs A)
     bool active = false, exhausted = false;
     uint32_t r = 0, cur = 0, steps = 0, inner_visits = 0, tri_tests = 0;
     int sp = -1;
-    uint32_t stack[STACK];
+    constexpr bool kSmemStack = RTA_SMEM_STACK && STACK <= 48;
+    __shared__ uint32_t s_stack[kSmemStack ? STACK * kTraceThreads : 1];
+    TraceStack<STACK, kSmemStack> stack;
+    stack.init(s_stack);
     Ray R;
     Best best;
     const NodeRec *nodes = nullptr;
