@@ -601,8 +601,9 @@ def run_gb300(args):
             frame_trace_ms.append(float(ft.value))
         torch.cuda.synchronize()
         L.check(lib.rta_frame_set_timing(fh, 0), "rta_frame_set_timing")
-        # primary trace kernel alone: the roofline kernel
-        trace_ms = []
+        # the primary rays alone, and the frame's bounce rays alone (rta_trace
+        # over the frame's bounce buffers), for per-pass rates
+        trace_ms, bounce_ms = [], []
         for _ in range(args.steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -613,6 +614,16 @@ def run_gb300(args):
             e1.record()
             e1.synchronize()
             trace_ms.append(e0.elapsed_time(e1))
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            L.check(lib.rta_trace(C.byref(bvh.view), C.c_void_p(frame.orig), C.c_void_p(frame.dir),
+                                  C.c_void_p(frame.maxt), nbounce, C.c_void_p(0), P._ptr(tmp), L.TRACE_CIS,
+                                  C.c_void_p(0), sh), "trace")
+            e1.record()
+            e1.synchronize()
+            bounce_ms.append(e0.elapsed_time(e1))
     clk.mark(False)
     clk.__exit__(None, None, None)
     if pg:
@@ -728,6 +739,9 @@ def run_gb300(args):
                   "algorithmic_bytes": 372 * n, "achieved_gbs": 372 * n / (bmean * 1e-3) / 1e9,
                   "frac_of_peak": 372 * n / (bmean * 1e-3) / 1e9 / peak},
         "trace": {"primary_ms": tr_ms, "primary_mrays_s": nrays / (tr_ms * 1e-3) / 1e6,
+                  "bounce_ms": statistics.mean(bounce_ms),
+                  "bounce_mrays_s": nbounce / (statistics.mean(bounce_ms) * 1e-3) / 1e6,
+                  "combined_mrays_s": value,
                   "primary_algorithmic_gbs": prim_bytes / (tr_ms * 1e-3) / 1e9,
                   "inner_visits_per_ray": inner_visits / rays_per_step,
                   "tri_tests_per_ray": tri_tests / rays_per_step,
