@@ -10,9 +10,13 @@ separately in the same run and reported under "build".
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-value  = rays traced per second over the frame's kernels (device-resident rays)
-e2e    = the same frame through the C ABI with host rays: pinned host -> device
-         copy of the primary rays, the frame, device -> host copy of all hits
+value  = rays traced per second over the frame's kernels (device-resident rays;
+         the frame is the fused trace launch + the bounce gather)
+e2e    = the same frame through the C ABI with host rays, one
+         rta_host_frames_run per step: pinned host -> device copy of the primary
+         rays, the frame, device -> host copy of all hits and the bounce count;
+         the copies run on their own streams beside the neighbouring steps
+roofline = the fused frame kernel, timed by events rta_frame_run records
 N > 1  = independent replicas, one per GPU (weak scaling); the time is the max
          over ranks.
 """
