@@ -245,10 +245,10 @@ __global__ void k_to_2f4(const NodeRec *__restrict__ nodes, const RootRec *__res
         const uint32_t pl = parents[k];
         const NodeRec *nd = nodes + (pl >> 1);
         const float *f = reinterpret_cast<const float *>(nd);
-        const int o = (pl & 1u) ? 6 : 0;
-        lo[0] = f[o + 0]; hi[0] = f[o + 1];
-        lo[1] = f[o + 2]; hi[1] = f[o + 3];
-        lo[2] = f[o + 4]; hi[2] = f[o + 5];
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = f[slot_lo(pl & 1u, a)];
+            hi[a] = f[slot_hi(pl & 1u, a)];
+        }
         link = reinterpret_cast<const uint32_t *>(&nd->q3)[pl & 1u];
     }
     uint32_t w0, w1;

@@ -5,10 +5,13 @@
 //   NodeRec  64 B per inner node i in [0, n-2] (the reference numbers inner
 //            nodes 0..n-2 and leaves n-1..2n-2, lbvh-kernels.cu:197-203).  A
 //            node stores the boxes and links of BOTH children, so the
-//            child-is test of an inner node is one 64-byte fetch:
-//              q0 = left  (lo.x, hi.x, lo.y, hi.y)
-//              q1 = left  (lo.z, hi.z), right (lo.x, hi.x)
-//              q2 = right (lo.y, hi.y, lo.z, hi.z)
+//            child-is test of an inner node is one 64-byte fetch.  The
+//            planes are interleaved left / right, so each 64-bit half of
+//            q0..q2 holds one plane of both children (the operand pair of
+//            one paired f32x2 instruction):
+//              q0 = (left lo.x, right lo.x, left hi.x, right hi.x)
+//              q1 = (left lo.y, right lo.y, left hi.y, right hi.y)
+//              q2 = (left lo.z, right lo.z, left hi.z, right hi.z)
 //              q3 = (left link, right link, left size, right size)
 //            size = number of triangles under the child (its Morton range).
 //            A left child's range ends at its node index and a right child's
@@ -41,6 +44,13 @@ struct __align__(16) NodeRec {
     uint4 q3;
 };
 static_assert(sizeof(NodeRec) == 64, "node record");
+
+// float offsets in a NodeRec of child `side`'s (0 left, 1 right) planes
+__host__ __device__ __forceinline__ int slot_lo(uint32_t side, int axis) { return 4 * axis + (int)side; }
+__host__ __device__ __forceinline__ int slot_hi(uint32_t side, int axis) { return 4 * axis + 2 + (int)side; }
+// a child's box as the argument list (lo.x, hi.x, lo.y, hi.y, lo.z, hi.z)
+#define RTA_LEFT_BOX(nd) (nd).q0.x, (nd).q0.z, (nd).q1.x, (nd).q1.z, (nd).q2.x, (nd).q2.z
+#define RTA_RIGHT_BOX(nd) (nd).q0.y, (nd).q0.w, (nd).q1.y, (nd).q1.w, (nd).q2.y, (nd).q2.w
 
 struct __align__(16) RootRec {
     float lo[3], hi[3];

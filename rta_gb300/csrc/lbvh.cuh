@@ -417,19 +417,21 @@ __device__ __forceinline__ void write_slot(NodeRec *nd, uint32_t side, const flo
                                            const float hi[3])
 {
     float *f = reinterpret_cast<float *>(nd);
-    const int o = side ? 6 : 0;
-    f[o + 0] = lo[0]; f[o + 1] = hi[0];
-    f[o + 2] = lo[1]; f[o + 3] = hi[1];
-    f[o + 4] = lo[2]; f[o + 5] = hi[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        f[slot_lo(side, k)] = lo[k];
+        f[slot_hi(side, k)] = hi[k];
+    }
 }
 
 __device__ __forceinline__ void read_slot_cg(const NodeRec *nd, uint32_t side, float lo[3], float hi[3])
 {
     const float *f = reinterpret_cast<const float *>(nd);
-    const int o = side ? 6 : 0;
-    lo[0] = __ldcg(f + o + 0); hi[0] = __ldcg(f + o + 1);
-    lo[1] = __ldcg(f + o + 2); hi[1] = __ldcg(f + o + 3);
-    lo[2] = __ldcg(f + o + 4); hi[2] = __ldcg(f + o + 5);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = __ldcg(f + slot_lo(side, k));
+        hi[k] = __ldcg(f + slot_hi(side, k));
+    }
 }
 
 // Arrival count with acquire-release semantics at device scope: the first

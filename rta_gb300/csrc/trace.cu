@@ -41,38 +41,58 @@ struct TraceArgs {
     uint32_t *b_flag;
 };
 
-// Per-ray constants of the slab test: the ray and which direction components
-// are zero (intersect_aabb treats d == 0 separately).
+// three-input min / max (sm_100 family); NaN inputs are ignored as by fminf / fmaxf
+__device__ __forceinline__ float max3f(float a, float b, float c)
+{
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c)
+{
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// Per-ray constants of the slab test: the ray, which direction components
+// are zero (intersect_aabb treats d == 0 separately) and the constants of the
+// division-free filter below.
 struct Ray {
     float o[3], d[3];
     uint32_t zero;   // bit k: d[k] == 0
     float tmax;
-    float rd[3];     // RN(1 / d[k]) for the slab filter
-    float ord[3];    // RN(o[k] * rd[k]): the filter's quotients are fma(plane, rd, -ord)
-    float eabs;      // absolute error term of those quotients, max |ord[k]| 2^-23 (+ 2^-146)
-    bool fast;       // the slab filter applies (every nonzero |d[k]| in [2^-100, 2^100])
+    float tmax_up;   // least float above tmax (+inf for a NaN tmax): t > tmax <=> t >= tmax_up
+    float eabs;      // absolute error term of the filter's quotients, max |o[k] rd[k]| 2^-23 (+ 2^-146)
+    bool fast;       // the filter applies: every |d[k]| in [2^-100, 2^100], o[k] rd[k] finite
+    float rd[3];     // RN(1 / d[k]); the filter's quotients are fma(plane, rd[k], nord[k])
+    float nord[3];   // -RN(o[k] rd[k])
 };
 
 __device__ __forceinline__ void make_ray(Ray &R, const float o[3], const float d[3], float tmax)
 {
     R.zero = 0;
-    R.fast = true;
+    bool fast = true;
+    float eabs = 1.12103877e-44f;   // 2^-146
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         R.o[k] = o[k];
         R.d[k] = d[k];
         if (d[k] == 0.0f) R.zero |= 1u << k;
         const float ad = fabsf(d[k]);
-        R.fast = R.fast && (d[k] == 0.0f || (ad >= 7.8886091e-31f && ad <= 1.2676506e30f));
-        R.rd[k] = d[k] == 0.0f ? 0.0f : __frcp_rn(d[k]);
+        fast = fast && ad >= 7.8886091e-31f && ad <= 1.2676506e30f;   // also false for 0, NaN, inf
+        const float rd = d[k] == 0.0f ? 0.0f : __frcp_rn(d[k]);
+        const float ord = __fmul_rn(o[k], rd);
+        fast = fast && fabsf(ord) <= FLT_MAX;
+        eabs = fmaxf(eabs, __fmaf_ru(fabsf(ord), 1.19209290e-07f, 1.12103877e-44f));
+        R.rd[k] = rd;
+        R.nord[k] = -ord;
     }
     R.tmax = tmax;
-    R.eabs = 1.12103877e-44f;   // 2^-146
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        R.ord[k] = __fmul_rn(o[k], R.rd[k]);
-        R.eabs = fmaxf(R.eabs, __fmaf_ru(fabsf(R.ord[k]), 1.19209290e-07f, 1.12103877e-44f));
-    }
+    // RU(tmax + 2^-149) is the next float up for every finite tmax (and +inf for +inf)
+    R.tmax_up = tmax != tmax ? __int_as_float(0x7f800000) : (tmax < -FLT_MAX ? -FLT_MAX : __fadd_ru(tmax, 1.40129846e-45f));
+    R.eabs = eabs;
+    R.fast = fast;
 }
 
 // intersect_aabb (librta/intersect.h:56-150).  The reference walks the axes
@@ -126,42 +146,47 @@ __device__ __forceinline__ bool slab_test(float lx, float hx, float ly, float hy
 // are rounded outward.  A decision is taken from the intervals when it is the
 // same for every value in them; otherwise the step falls back to the exact
 // divisions.  NaN bounds (overflowing quotients) always count as uncertain.
+// The filter applies to rays without a zero direction component and with
+// finite o * r (R.fast); the others take the exact test at every step.  On
+// the 1080p terrain frame the exact fallback runs in 0.03 % of the child-is
+// steps (0.5 % of warp iterations).
 #ifndef RTA_SLAB_FILTER
 #define RTA_SLAB_FILTER 1
 #endif
 constexpr float kFilterRel = 4.76837158e-07f;   // 2^-21
 constexpr float kFilterAbs = 1.12103877e-44f;   // 2^-146
 
+// The decision from outward-rounded bounds of t_near and t_far.  cull =
+// min(best t, tmax_up): "t_near >= best t or t_near > tmax" is t_near >= cull.
 // 0: certainly not a kept hit; 1: certainly a kept hit; 2: uncertain.
 // [lo, hi] bounds the exact t_near when the child is kept.
-__device__ __forceinline__ int slab_filter(float lx, float hx, float ly, float hy, float lz, float hz,
-                                           const Ray &R, float best_t, float &lo, float &hi)
+__device__ __forceinline__ int filter_bounds(float tn_lo, float tn_hi, float tf_lo, float tf_hi, float cull,
+                                             float &lo, float &hi)
 {
-    const float bl[3] = {lx, ly, lz}, bh[3] = {hx, hy, hz};
-    float tn = -FLT_MAX, tf = FLT_MAX;
-    bool inside = true;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        if (R.zero & (1u << k)) {
-            inside = inside && !(R.o[k] < bl[k] || R.o[k] > bh[k]);
-        } else {
-            const float q1 = __fmaf_rn(bl[k], R.rd[k], -R.ord[k]);
-            const float q2 = __fmaf_rn(bh[k], R.rd[k], -R.ord[k]);
-            tn = fmaxf(tn, fminf(q1, q2));
-            tf = fminf(tf, fmaxf(q1, q2));
-        }
-    }
-    if (!inside) return 0;
-    const float wn = __fmaf_ru(fabsf(tn), kFilterRel, R.eabs);
-    const float wf = __fmaf_ru(fabsf(tf), kFilterRel, R.eabs);
-    const float tn_lo = __fsub_rd(tn, wn), tn_hi = __fadd_ru(tn, wn);
-    const float tf_lo = __fsub_rd(tf, wf), tf_hi = __fadd_ru(tf, wf);
-    // hit = t_near <= t_far && t_far >= 0; kept = hit && !(t_near >= best_t) && !(t_near > t_max)
-    if (tn_lo > tf_hi || tf_hi < 0.0f || tn_lo >= best_t || tn_lo > R.tmax) return 0;   // certainly not
+    // hit = t_near <= t_far && t_far >= 0; kept = hit && t_near < cull
+    if (tn_lo > tf_hi || tf_hi < 0.0f || tn_lo >= cull) return 0;   // certainly not
     lo = tn_lo;
     hi = tn_hi;
-    if (tn_hi <= tf_lo && tf_lo >= 0.0f && tn_hi < best_t && tn_hi <= R.tmax) return 1;  // certainly
+    if (tn_hi <= tf_lo && tf_lo >= 0.0f && tn_hi < cull) return 1;   // certainly
     return 2;
+}
+
+// One box; R.fast is a precondition (no zero direction component).  t_near
+// and t_far as max / min over the axes need no -FLT_MAX / FLT_MAX start: a
+// quotient of +-inf (overflow) makes the bounds inf or NaN, which decide
+// nothing certain unless the other, finite, distance does.
+__device__ __forceinline__ int slab_filter(float lx, float hx, float ly, float hy, float lz, float hz,
+                                           const Ray &R, float cull, float &lo, float &hi)
+{
+    const float qlx = __fmaf_rn(lx, R.rd[0], R.nord[0]), qhx = __fmaf_rn(hx, R.rd[0], R.nord[0]);
+    const float qly = __fmaf_rn(ly, R.rd[1], R.nord[1]), qhy = __fmaf_rn(hy, R.rd[1], R.nord[1]);
+    const float qlz = __fmaf_rn(lz, R.rd[2], R.nord[2]), qhz = __fmaf_rn(hz, R.rd[2], R.nord[2]);
+    const float tn = max3f(fminf(qlx, qhx), fminf(qly, qhy), fminf(qlz, qhz));
+    const float tf = min3f(fmaxf(qlx, qhx), fmaxf(qly, qhy), fmaxf(qlz, qhz));
+    const float wn = __fmaf_ru(fabsf(tn), kFilterRel, R.eabs);
+    const float wf = __fmaf_ru(fabsf(tf), kFilterRel, R.eabs);
+    return filter_bounds(__fsub_rd(tn, wn), __fadd_ru(tn, wn), __fsub_rd(tf, wf), __fadd_ru(tf, wf), cull, lo,
+                         hi);
 }
 
 // The entry distance of one box from its near planes: the approximate
@@ -176,9 +201,9 @@ __device__ __forceinline__ bool entry_axis(float lx, float hx, float ly, float h
 {
     const float c0 = R.d[0] > 0.0f ? lx : hx, c1 = R.d[1] > 0.0f ? ly : hy, c2 = R.d[2] > 0.0f ? lz : hz;
     const float a0 = __fsub_rn(c0, R.o[0]), a1 = __fsub_rn(c1, R.o[1]), a2 = __fsub_rn(c2, R.o[2]);
-    const float q0 = (R.zero & 1u) ? -FLT_MAX : __fmul_rn(a0, R.rd[0]);
-    const float q1 = (R.zero & 2u) ? -FLT_MAX : __fmul_rn(a1, R.rd[1]);
-    const float q2 = (R.zero & 4u) ? -FLT_MAX : __fmul_rn(a2, R.rd[2]);
+    const float q0 = __fmul_rn(a0, R.rd[0]);
+    const float q1 = __fmul_rn(a1, R.rd[1]);
+    const float q2 = __fmul_rn(a2, R.rd[2]);
     const bool k2 = q2 >= fmaxf(q0, q1);
     const bool k1 = !k2 && q1 >= q0;
     const float top = k2 ? q2 : (k1 ? q1 : q0);
@@ -189,7 +214,7 @@ __device__ __forceinline__ bool entry_axis(float lx, float hx, float ly, float h
     den = k2 ? R.d[2] : (k1 ? R.d[1] : R.d[0]);
     const float wt = __fmaf_ru(fabsf(top), kFilterRel, kFilterAbs);
     const float ws = __fmaf_ru(fabsf(second), kFilterRel, kFilterAbs);
-    return top != -FLT_MAX && __fadd_ru(second, ws) < __fsub_rd(top, wt);
+    return __fadd_ru(second, ws) < __fsub_rd(top, wt);
 }
 
 // dl <= dr for two kept children whose entry intervals overlap: equal planes
@@ -199,8 +224,8 @@ __device__ __forceinline__ bool order_resolve(const NodeRec &nd, const Ray &R, b
 {
     int kl, kr;
     float cl, cr, nl, nr, dl_den, dr_den;
-    if (!entry_axis(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, kl, cl, nl, dl_den)) return false;
-    if (!entry_axis(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, kr, cr, nr, dr_den)) return false;
+    if (!entry_axis(RTA_LEFT_BOX(nd), R, kl, cl, nl, dl_den)) return false;
+    if (!entry_axis(RTA_RIGHT_BOX(nd), R, kr, cr, nr, dr_den)) return false;
     if (kl == kr && __float_as_uint(cl) == __float_as_uint(cr)) {
         left_first = true;
         return true;
@@ -216,8 +241,9 @@ __device__ __forceinline__ void cis_decide(const NodeRec &nd, const Ray &R, floa
 {
     if (RTA_SLAB_FILTER && R.fast) {
         float llo = 0.f, lhi = 0.f, rlo = 0.f, rhi = 0.f;
-        const int sl = slab_filter(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, best_t, llo, lhi);
-        const int sr = slab_filter(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, best_t, rlo, rhi);
+        const float cull = fminf(best_t, R.tmax_up);
+        const int sl = slab_filter(RTA_LEFT_BOX(nd), R, cull, llo, lhi);
+        const int sr = slab_filter(RTA_RIGHT_BOX(nd), R, cull, rlo, rhi);
         if (sl != 2 && sr != 2) {
             hl = sl == 1;
             hr = sr == 1;
@@ -237,8 +263,8 @@ __device__ __forceinline__ void cis_decide(const NodeRec &nd, const Ray &R, floa
         }
     }
     float dl = FLT_MAX, dr = FLT_MAX;
-    hl = slab_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, dl);
-    hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, dr);
+    hl = slab_test(RTA_LEFT_BOX(nd), R, dl);
+    hr = slab_test(RTA_RIGHT_BOX(nd), R, dr);
     if (dl >= best_t || dl > R.tmax) hl = false;
     if (dr >= best_t || dr > R.tmax) hr = false;
     left_first = dl <= dr;
@@ -408,13 +434,15 @@ template <int STACK> struct TraceStack<STACK, true> {
 #define RTA_LEAF_PARK 4
 #endif
 
-// blocks per SM the compiler must fit (0: no register cap)
+// blocks per SM the compiler must fit in registers for the child-is kernels
+// (8 = 64 registers: full occupancy beats the few spilled bytes, 3 % on the
+// 1080p frame; the direct-is / Aila kernels keep their register count)
 #ifndef RTA_TRACE_MIN_BLOCKS
-#define RTA_TRACE_MIN_BLOCKS 0
+#define RTA_TRACE_MIN_BLOCKS 8
 #endif
 
 template <bool DIS, bool SHADOW, bool AILA, bool STATS, int STACK, bool FUSE = false>
-__global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(TraceArgs A)
+__global__ void __launch_bounds__(kTraceThreads, (!DIS && !AILA) ? RTA_TRACE_MIN_BLOCKS : 0) k_trace(TraceArgs A)
 {
     static_assert(!FUSE || (!DIS && !SHADOW && !AILA && !STATS), "the fused frame is child-is closest hit");
     const uint32_t lane = threadIdx.x & 31u;
@@ -511,8 +539,8 @@ __global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(T
                     bool hl, hr, left_first;
                     if (AILA) {
                         float dl = FLT_MAX, dr = FLT_MAX;
-                        hl = aila_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R.o, id, best.t, dl);
-                        hr = aila_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R.o, id, best.t, dr);
+                        hl = aila_test(RTA_LEFT_BOX(nd), R.o, id, best.t, dl);
+                        hr = aila_test(RTA_RIGHT_BOX(nd), R.o, id, best.t, dr);
                         if (dl >= best.t || dl > R.tmax) hl = false;
                         if (dr >= best.t || dr > R.tmax) hr = false;
                         left_first = dl <= dr;
@@ -559,7 +587,8 @@ __global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(T
                 int certain = 2;
                 if (!AILA && RTA_SLAB_FILTER && R.fast) {
                     float lo, hi;
-                    certain = slab_filter(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], R, best.t, lo, hi);
+                    certain = slab_filter(bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], R, fminf(best.t, R.tmax_up), lo,
+                                          hi);
                 }
                 if (certain != 2) {
                     h = certain == 1;
@@ -580,8 +609,8 @@ __global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(T
                         const NodeRec nd = load_node(A.nodes, cur);
                         stack[++sp] = (cur << 1) | 1u;
                         cur = nd.q3.x;
-                        bx[0] = nd.q0.x; bx[1] = nd.q0.y; bx[2] = nd.q0.z;
-                        bx[3] = nd.q0.w; bx[4] = nd.q1.x; bx[5] = nd.q1.y;
+                        bx[0] = nd.q0.x; bx[1] = nd.q0.z; bx[2] = nd.q1.x;
+                        bx[3] = nd.q1.z; bx[4] = nd.q2.x; bx[5] = nd.q2.z;
                     }
                 } else {
                     pop = true;
@@ -604,12 +633,12 @@ __global__ void __launch_bounds__(kTraceThreads, RTA_TRACE_MIN_BLOCKS) k_trace(T
                         const NodeRec nd = load_node(A.nodes, e >> 1);
                         if (e & 1u) {
                             cur = nd.q3.y;
-                            bx[0] = nd.q1.z; bx[1] = nd.q1.w; bx[2] = nd.q2.x;
-                            bx[3] = nd.q2.y; bx[4] = nd.q2.z; bx[5] = nd.q2.w;
+                            bx[0] = nd.q0.y; bx[1] = nd.q0.w; bx[2] = nd.q1.y;
+                            bx[3] = nd.q1.w; bx[4] = nd.q2.y; bx[5] = nd.q2.w;
                         } else {
                             cur = nd.q3.x;
-                            bx[0] = nd.q0.x; bx[1] = nd.q0.y; bx[2] = nd.q0.z;
-                            bx[3] = nd.q0.w; bx[4] = nd.q1.x; bx[5] = nd.q1.y;
+                            bx[0] = nd.q0.x; bx[1] = nd.q0.z; bx[2] = nd.q1.x;
+                            bx[3] = nd.q1.z; bx[4] = nd.q2.x; bx[5] = nd.q2.z;
                         }
                     }
                 }
@@ -969,8 +998,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
                     at_inner = true;
                     ++inner_visits;
                     nd = load_node(A.nodes, cur);
-                    hl = slab_test(nd.q0.x, nd.q0.y, nd.q0.z, nd.q0.w, nd.q1.x, nd.q1.y, R, tnl, tfl);
-                    hr = slab_test(nd.q1.z, nd.q1.w, nd.q2.x, nd.q2.y, nd.q2.z, nd.q2.w, R, tnr, tfr);
+                    hl = slab_test(RTA_LEFT_BOX(nd), R, tnl, tfl);
+                    hr = slab_test(RTA_RIGHT_BOX(nd), R, tnr, tfr);
                     if (tnl >= best.t || tnl > R.tmax) hl = false;
                     if (tnr >= best.t || tnr > R.tmax) hr = false;
                     // only overlapping entry-exit intervals make the order
