@@ -463,28 +463,57 @@ __global__ void __launch_bounds__(kTraceThreads, (!DIS && !AILA) ? RTA_TRACE_MIN
     Best best;
     float bx[6];   // DIS: box of the current node
     bool overflow = false, capped = false, bad = false;
-    bool second = false;   // FUSE: the lane traces ray r's bounce ray
+    bool second = false;    // FUSE: the lane traces ray r's bounce ray
+    bool pending = false;   // FUSE: ray r hit; its bounce ray is made at the next fetch
 
     for (;;) {
+        // idle lanes (pending ones included) take new rays together once
+        // kFetchIdle of them are idle: a pending lane its own bounce ray, the
+        // others rays from the queue.  The branch is warp-uniform.
         const uint32_t idle = __ballot_sync(0xffffffffu, !active);
-        if (!exhausted && __popc(idle) >= kFetchIdle) {
-            const int leader = __ffs(idle) - 1;
+        const uint32_t pend = FUSE ? __ballot_sync(0xffffffffu, pending) : 0u;
+        if ((__popc(idle) >= kFetchIdle && (!exhausted || pend != 0u)) || (pend != 0u && idle == 0xffffffffu)) {
+            const uint32_t want = idle & ~pend;
+            bool queued = false;
             uint32_t base = 0;
-            if ((int)lane == leader) base = atomicAdd(A.queue, (uint32_t)__popc(idle));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (base >= nrays) {
-                exhausted = true;
-            } else if (!active) {
-                r = base + __popc(idle & lt_mask);
-                if (r < nrays) {
-                    float o[3], d[3];
-                    o[0] = A.orig[3 * (size_t)r + 0];
-                    o[1] = A.orig[3 * (size_t)r + 1];
-                    o[2] = A.orig[3 * (size_t)r + 2];
-                    d[0] = A.dir[3 * (size_t)r + 0];
-                    d[1] = A.dir[3 * (size_t)r + 1];
-                    d[2] = A.dir[3 * (size_t)r + 2];
-                    make_ray(R, o, d, A.maxt[r]);
+            if (!exhausted && want != 0u) {
+                const int leader = __ffs(want) - 1;
+                if ((int)lane == leader) base = atomicAdd(A.queue, (uint32_t)__popc(want));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (base >= nrays) exhausted = true;
+                else queued = true;
+            }
+            if (!active) {
+                float o[3], d[3], tmax = FLT_MAX;
+                bool got = false;
+                if (FUSE && pending) {
+                    // the bounce ray of ray r's hit (bounce.cuh)
+                    bounce_ray(load_tri(A.tris, best.ref), R.o, R.d, best.t, r, A.seed, A.eps, o, d);
+                    A.b_orig[3 * (size_t)r + 0] = o[0];
+                    A.b_orig[3 * (size_t)r + 1] = o[1];
+                    A.b_orig[3 * (size_t)r + 2] = o[2];
+                    A.b_dir[3 * (size_t)r + 0] = d[0];
+                    A.b_dir[3 * (size_t)r + 1] = d[1];
+                    A.b_dir[3 * (size_t)r + 2] = d[2];
+                    pending = false;
+                    second = true;
+                    got = true;
+                } else if (queued) {
+                    r = base + __popc(want & lt_mask);
+                    if (r < nrays) {
+                        o[0] = A.orig[3 * (size_t)r + 0];
+                        o[1] = A.orig[3 * (size_t)r + 1];
+                        o[2] = A.orig[3 * (size_t)r + 2];
+                        d[0] = A.dir[3 * (size_t)r + 0];
+                        d[1] = A.dir[3 * (size_t)r + 1];
+                        d[2] = A.dir[3 * (size_t)r + 2];
+                        tmax = A.maxt[r];
+                        second = false;
+                        got = true;
+                    }
+                }
+                if (got) {
+                    make_ray(R, o, d, tmax);
                     if (AILA) {
                         const float ooeps = 8.27180612553027674871e-25f;   // exp2f(-80)
 #pragma unroll
@@ -501,7 +530,6 @@ __global__ void __launch_bounds__(kTraceThreads, (!DIS && !AILA) ? RTA_TRACE_MIN
                         bx[0] = root.lo[0]; bx[1] = root.hi[0]; bx[2] = root.lo[1];
                         bx[3] = root.hi[1]; bx[4] = root.lo[2]; bx[5] = root.hi[2];
                     }
-                    second = false;
                     active = true;
                 }
             }
@@ -659,27 +687,8 @@ __global__ void __launch_bounds__(kTraceThreads, (!DIS && !AILA) ? RTA_TRACE_MIN
                 }
                 const bool bounce = !second && best.t != FLT_MAX && best.ref < A.n_tris;
                 if (!second) A.b_flag[r] = bounce ? 1u : 0u;
-                if (bounce) {
-                    // the bounce ray of this hit (bounce.cuh), traced next by this lane
-                    float bo[3], bd[3];
-                    bounce_ray(load_tri(A.tris, best.ref), R.o, R.d, best.t, r, A.seed, A.eps, bo, bd);
-                    A.b_orig[3 * (size_t)r + 0] = bo[0];
-                    A.b_orig[3 * (size_t)r + 1] = bo[1];
-                    A.b_orig[3 * (size_t)r + 2] = bo[2];
-                    A.b_dir[3 * (size_t)r + 0] = bd[0];
-                    A.b_dir[3 * (size_t)r + 1] = bd[1];
-                    A.b_dir[3 * (size_t)r + 2] = bd[2];
-                    make_ray(R, bo, bd, FLT_MAX);
-                    best.t = FLT_MAX;
-                    best.beta = best.gamma = 0.f;
-                    best.ref = 0;
-                    sp = -1;
-                    steps = 0;
-                    cur = root.link;
-                    second = true;
-                } else {
-                    active = false;
-                }
+                pending = bounce;
+                active = false;
             } else {
                 if (best.t != FLT_MAX) {
                     reinterpret_cast<float4 *>(A.hits)[r] =
