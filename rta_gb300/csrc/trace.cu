@@ -234,31 +234,49 @@ __device__ __forceinline__ bool order_resolve(const NodeRec &nd, const Ray &R, b
     return true;
 }
 
+// Outward-rounded bounds of one box's t_near and t_far from the approximate
+// quotients (R.fast is a precondition).
+__device__ __forceinline__ void slab_bounds(float lx, float hx, float ly, float hy, float lz, float hz,
+                                            const Ray &R, float &tn_lo, float &tn_hi, float &tf_lo, float &tf_hi)
+{
+    const float qlx = __fmaf_rn(lx, R.rd[0], R.nord[0]), qhx = __fmaf_rn(hx, R.rd[0], R.nord[0]);
+    const float qly = __fmaf_rn(ly, R.rd[1], R.nord[1]), qhy = __fmaf_rn(hy, R.rd[1], R.nord[1]);
+    const float qlz = __fmaf_rn(lz, R.rd[2], R.nord[2]), qhz = __fmaf_rn(hz, R.rd[2], R.nord[2]);
+    const float tn = max3f(fminf(qlx, qhx), fminf(qly, qhy), fminf(qlz, qhz));
+    const float tf = min3f(fmaxf(qlx, qhx), fmaxf(qly, qhy), fmaxf(qlz, qhz));
+    const float wn = __fmaf_ru(fabsf(tn), kFilterRel, R.eabs);
+    const float wf = __fmaf_ru(fabsf(tf), kFilterRel, R.eabs);
+    tn_lo = __fsub_rd(tn, wn);
+    tn_hi = __fadd_ru(tn, wn);
+    tf_lo = __fsub_rd(tf, wf);
+    tf_hi = __fadd_ru(tf, wf);
+}
+
 // The child-is decisions of one node: hl / hr (child hit and not culled) and
-// left_first (dl <= dr); exact, through the filter where it is certain.
+// left_first, the child to visit first among the kept ones (dl <= dr when
+// both are kept); exact, through the filter where it is certain.  The
+// filter's "certainly kept" and "certainly not" are predicates, never both
+// true (certainly kept implies tn_lo <= tn_hi <= tf_lo <= tf_hi, tf_lo >= 0
+// and tn_lo <= tn_hi < cull).
 __device__ __forceinline__ void cis_decide(const NodeRec &nd, const Ray &R, float best_t, bool &hl, bool &hr,
                                            bool &left_first)
 {
     if (RTA_SLAB_FILTER && R.fast) {
-        float llo = 0.f, lhi = 0.f, rlo = 0.f, rhi = 0.f;
         const float cull = fminf(best_t, R.tmax_up);
-        const int sl = slab_filter(RTA_LEFT_BOX(nd), R, cull, llo, lhi);
-        const int sr = slab_filter(RTA_RIGHT_BOX(nd), R, cull, rlo, rhi);
-        if (sl != 2 && sr != 2) {
-            hl = sl == 1;
-            hr = sr == 1;
-            if (!(hl && hr)) {
-                left_first = true;
-                return;
-            }
-            if (lhi <= rlo) {
-                left_first = true;
-                return;
-            }
-            if (llo > rhi) {
-                left_first = false;
-                return;
-            }
+        float lnl, lnh, lfl, lfh, rnl, rnh, rfl, rfh;
+        slab_bounds(RTA_LEFT_BOX(nd), R, lnl, lnh, lfl, lfh);
+        slab_bounds(RTA_RIGHT_BOX(nd), R, rnl, rnh, rfl, rfh);
+        // hit = t_near <= t_far && t_far >= 0; kept = hit && t_near < cull
+        const bool l_yes = lnh <= lfl && lfl >= 0.0f && lnh < cull;
+        const bool r_yes = rnh <= rfl && rfl >= 0.0f && rnh < cull;
+        const bool l_no = lnl > lfh || lfh < 0.0f || lnl >= cull;
+        const bool r_no = rnl > rfh || rfh < 0.0f || rnl >= cull;
+        if ((l_yes || l_no) && (r_yes || r_no)) {
+            hl = l_yes;
+            hr = r_yes;
+            // both kept: the entry intervals order them, else the exact entry
+            left_first = l_yes && (!r_yes || lnh <= rnl);
+            if (!(l_yes && r_yes) || lnh <= rnl || lnl > rnh) return;
             if (order_resolve(nd, R, left_first)) return;
         }
     }
@@ -267,7 +285,7 @@ __device__ __forceinline__ void cis_decide(const NodeRec &nd, const Ray &R, floa
     hr = slab_test(RTA_RIGHT_BOX(nd), R, dr);
     if (dl >= best_t || dl > R.tmax) hl = false;
     if (dr >= best_t || dr > R.tmax) hr = false;
-    left_first = dl <= dr;
+    left_first = hl && (!hr || dl <= dr);
 }
 
 // intersect_aabb_aila with the ailabox kernels' reciprocal (kernels.cu:966-970)
@@ -571,25 +589,21 @@ __global__ void __launch_bounds__(kTraceThreads, (!DIS && !AILA) ? RTA_TRACE_MIN
                         hr = aila_test(RTA_RIGHT_BOX(nd), R.o, id, best.t, dr);
                         if (dl >= best.t || dl > R.tmax) hl = false;
                         if (dr >= best.t || dr > R.tmax) hr = false;
-                        left_first = dl <= dr;
+                        left_first = hl && (!hr || dl <= dr);
                     } else {
                         cis_decide(nd, R, best.t, hl, hr, left_first);
                     }
-                    if (hl && hr) {
-                        if (sp + 1 >= STACK) {
-                            overflow = true;
-                            done = true;
-                        } else if (left_first) {
-                            stack[++sp] = nd.q3.y;
-                            cur = nd.q3.x;
-                        } else {
-                            stack[++sp] = nd.q3.x;
-                            cur = nd.q3.y;
+                    if (hl || hr) {
+                        // the first kept child next; with both kept the other one onto the stack
+                        cur = left_first ? nd.q3.x : nd.q3.y;
+                        if (hl && hr) {
+                            if (sp + 1 >= STACK) {
+                                overflow = true;
+                                done = true;
+                            } else {
+                                stack[++sp] = left_first ? nd.q3.y : nd.q3.x;
+                            }
                         }
-                    } else if (hl) {
-                        cur = nd.q3.x;
-                    } else if (hr) {
-                        cur = nd.q3.y;
                     } else if (sp < 0) {
                         done = true;
                     } else {
@@ -801,21 +815,17 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_batch(BatchTraceArgs A)
                 const NodeRec nd = load_node(nodes, cur);
                 bool hl, hr, left_first;
                 cis_decide(nd, R, best.t, hl, hr, left_first);
-                if (hl && hr) {
-                    if (sp + 1 >= STACK) {
-                        overflow = true;
-                        done = true;
-                    } else if (left_first) {
-                        stack[++sp] = nd.q3.y;
-                        cur = nd.q3.x;
-                    } else {
-                        stack[++sp] = nd.q3.x;
-                        cur = nd.q3.y;
+                if (hl || hr) {
+                    // the first kept child next; with both kept the other one onto the stack
+                    cur = left_first ? nd.q3.x : nd.q3.y;
+                    if (hl && hr) {
+                        if (sp + 1 >= STACK) {
+                            overflow = true;
+                            done = true;
+                        } else {
+                            stack[++sp] = left_first ? nd.q3.y : nd.q3.x;
+                        }
                     }
-                } else if (hl) {
-                    cur = nd.q3.x;
-                } else if (hr) {
-                    cur = nd.q3.y;
                 } else if (sp < 0) {
                     done = true;
                 } else {
