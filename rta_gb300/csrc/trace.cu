@@ -570,14 +570,15 @@ __global__ void __launch_bounds__(kTraceThreads, (!DIS && !AILA) ? RTA_TRACE_MIN
 
         // ---- one traversal step ----
         bool done = false;
-        if (++steps > kMaxSteps) {
-            capped = true;
-            done = true;
-        } else if (!DIS) {
-            // child-is (kernels.cu:797-852): test both children, nearer first
+        ++steps;
+        if (!DIS) {
+            // child-is (kernels.cu:797-852): test both children, nearer first.
+            // A broken link and a runaway ray share one rare branch; only
+            // inner steps push, so capping them bounds every ray.
             if (!is_leaf(cur)) {
-                if (cur >= n_inner) {
-                    bad = true;
+                if (cur >= n_inner || steps > kMaxSteps) {
+                    bad = bad || cur >= n_inner;
+                    capped = capped || cur < n_inner;
                     done = true;
                 } else {
                     ++inner_visits;
@@ -618,6 +619,9 @@ __global__ void __launch_bounds__(kTraceThreads, (!DIS && !AILA) ? RTA_TRACE_MIN
                 else
                     cur = stack[sp--];
             }
+        } else if (steps > kMaxSteps) {
+            capped = true;
+            done = true;
         } else {
             // direct-is (kernels.cu:506-545): a node's own box is tested when it
             // is visited; the stack holds (parent << 1 | side) and a popped
@@ -803,12 +807,11 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_batch(BatchTraceArgs A)
         if (!active) continue;
 
         bool done = false;
-        if (++steps > kMaxSteps) {
-            capped = true;
-            done = true;
-        } else if (!is_leaf(cur)) {
-            if (cur >= n_inner) {
-                bad = true;
+        ++steps;
+        if (!is_leaf(cur)) {
+            if (cur >= n_inner || steps > kMaxSteps) {   // as in k_trace
+                bad = bad || cur >= n_inner;
+                capped = capped || cur < n_inner;
                 done = true;
             } else {
                 ++inner_visits;
