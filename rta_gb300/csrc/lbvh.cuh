@@ -26,6 +26,7 @@ constexpr int kMaxPasses = 8;          // 63-bit keys at 8 bits per digit
 struct BuildState {
     float lo[3], hi[3], scale[3];
     uint32_t done;                 // bounds last-block ticket (self-resetting)
+    uint32_t refit_done;           // refit summary last-block ticket (self-resetting)
 };
 
 // Zeroed by one memset before every build.  hist holds the global digit
