@@ -102,7 +102,15 @@ constexpr uint32_t kStatValue = (1u << 30) - 1u;
 
 // Walks tile statuses backwards from tile-1 until an inclusive prefix is found;
 // returns the exclusive prefix of `tile` for one counter.  stat[t * stride]
-// is tile t's word.  Bounded: sets RTA_DEV_SPIN_TIMEOUT in *flags on give-up.
+// is tile t's word.  The words of up to kLookbackWindow predecessors are
+// loaded at once (independent loads, one latency) and consumed nearest
+// first; a word not yet written ends the window and is polled again.
+// Bounded: sets RTA_DEV_SPIN_TIMEOUT in *flags on give-up.
+#ifndef RTA_LOOKBACK_WINDOW
+#define RTA_LOOKBACK_WINDOW 8
+#endif
+constexpr int kLookbackWindow = RTA_LOOKBACK_WINDOW;
+
 __device__ __forceinline__ uint32_t lookback(const uint32_t *stat, uint32_t stride, uint32_t tile,
                                              uint32_t *flags)
 {
@@ -110,18 +118,32 @@ __device__ __forceinline__ uint32_t lookback(const uint32_t *stat, uint32_t stri
     int t = (int)tile - 1;
     uint32_t spins = 0;
     while (t >= 0) {
-        uint32_t s = ld_volatile(stat + (size_t)t * stride);
-        if ((s & ~kStatValue) == 0u) {
+        uint32_t s[kLookbackWindow];
+#pragma unroll
+        for (int w = 0; w < kLookbackWindow; ++w)
+            s[w] = t - w >= 0 ? ld_volatile(stat + (size_t)(t - w) * stride) : 0u;
+        int used = 0;
+        bool stop = false;
+#pragma unroll
+        for (int w = 0; w < kLookbackWindow; ++w) {
+            if (stop || t - w < 0) break;
+            const uint32_t v = s[w];
+            if ((v & ~kStatValue) == 0u) {
+                stop = true;   // not written yet: poll it again
+                break;
+            }
+            excl += v & kStatValue;
+            ++used;
+            if (v & kStatPrefix) return excl;
+        }
+        t -= used;
+        if (stop) {
             if (++spins > kSpinLimit) {
                 atomicOr(flags, RTA_DEV_SPIN_TIMEOUT);
                 break;
             }
-            __nanosleep(32);
-            continue;
+            if (used == 0) __nanosleep(32);
         }
-        excl += s & kStatValue;
-        if (s & kStatPrefix) break;
-        --t;
     }
     return excl;
 }
