@@ -1,7 +1,7 @@
 // build.cu -- LBVH construction on sm_103a.
 //
-// Pipeline (one stream, no host synchronisation, five kernels + one memset):
-//   memset   sort histograms, tile counters and look-back words
+// Pipeline (one stream, no host synchronisation, seven kernels + one memset):
+//   memset   sort histograms, tile counters, look-back words, refit list count
 //   bounds   positions -> centroids, scene box (last-block reduction)
 //            [initTriangles + calculateVoxelBounds, lbvh-kernels.cu:344-359, 496-535]
 //   morton   centroids -> codes, digit histograms of every sort pass
@@ -11,7 +11,9 @@
 //            [thrust::sort_by_key, lbvh-kernels.cu:537-555]
 //   karras   radix-tree links + parent links; Morton-ordered triangles
 //            [build_tree_karras, :186-256; permutation, :557-578]
-//   refit    bottom-up boxes with equal-code leaf collapse
+//   refit    node boxes as unions over Morton ranges, equal-code leaf
+//            collapse (three kernels: segments, their summary, the nodes
+//            that cross segment borders)
 //            [build_bounding_boxes_karras2, :258-341]
 #include <cstdio>
 #include <cstring>
@@ -368,7 +370,8 @@ template <typename Key>
 __global__ void __launch_bounds__(kRefitSeg)
 k_refit_seg(const Key *__restrict__ codes, uint32_t n, NodeRec *__restrict__ nodes,
             const uint32_t *__restrict__ parents, TriRec *__restrict__ tris, float *__restrict__ pre,
-            float *__restrict__ suf, float *__restrict__ seg, uint32_t *__restrict__ flags)
+            float *__restrict__ suf, float *__restrict__ seg, uint32_t *__restrict__ cross,
+            uint32_t *__restrict__ n_cross, uint32_t *__restrict__ flags)
 {
     __shared__ float s_t[kRefitLevels][6][kRefitSeg];
     SegTable T{s_t};
@@ -377,27 +380,34 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n, NodeRec *__restrict__ nod
     Box6 b{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     if (j < n) b = leaf_box(tris[j]);
     T.build(b);
-    if (j >= n) return;
-    gstore(pre, j, T.query(0u, t));
-    gstore(suf, j, T.query(t, cnt - 1u));
-    if (t == 0u) gstore(seg, blockIdx.x, T.query(0u, cnt - 1u));
-    if (n == 1u) return;
-    // the leaf's box into its parent's record
-    const uint32_t pl = parents[n - 1u + j];
-    if ((pl >> 1) >= n - 1u) {
-        atomicOr(flags, RTA_DEV_BAD_LINK);
-    } else {
-        write_slot(nodes + (pl >> 1), pl & 1u, b.lo, b.hi);
-    }
-    // inner node j when its range lies in this segment (j is one end of it)
-    if (j + 1u < n) {
-        uint32_t l, r;
-        if (!node_range(nodes[j].q3, n, l, r)) {
-            atomicOr(flags, RTA_DEV_BAD_LINK);
-            return;
+    bool crosses = false;
+    if (j < n) {
+        gstore(pre, j, T.query(0u, t));
+        gstore(suf, j, T.query(t, cnt - 1u));
+        if (t == 0u) gstore(seg, blockIdx.x, T.query(0u, cnt - 1u));
+        if (n > 1u) {
+            // the leaf's box into its parent's record
+            const uint32_t pl = parents[n - 1u + j];
+            if ((pl >> 1) >= n - 1u) atomicOr(flags, RTA_DEV_BAD_LINK);
+            else write_slot(nodes + (pl >> 1), pl & 1u, b.lo, b.hi);
         }
-        if ((l / kRefitSeg) == (r / kRefitSeg) && j != 0u)
-            place_node(codes, n, j, l, r, T.query(l - base, r - base), nodes, parents, tris, flags);
+        // inner node j (one end of its range): here when the range lies in this
+        // segment, else on the list for k_refit_ext (the root is k_refit_top's)
+        uint32_t l, r;
+        if (j + 1u < n && j != 0u) {
+            if (!node_range(nodes[j].q3, n, l, r)) atomicOr(flags, RTA_DEV_BAD_LINK);
+            else if (l / kRefitSeg == r / kRefitSeg)
+                place_node(codes, n, j, l, r, T.query(l - base, r - base), nodes, parents, tris, flags);
+            else crosses = true;
+        }
+    }
+    const uint32_t lane = t & 31u, bm = __ballot_sync(0xffffffffu, crosses);
+    if (bm != 0u) {
+        const int leader = __ffs(bm) - 1;
+        uint32_t at = 0;
+        if ((int)lane == leader) at = atomicAdd(n_cross, (uint32_t)__popc(bm));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (crosses) cross[at + __popc(bm & ((1u << lane) - 1u))] = j;
     }
 }
 
@@ -466,19 +476,19 @@ __device__ __forceinline__ Box6 t1_query(const float *t1, uint32_t nseg, uint32_
     return box_join(gload(lv, a), gload(lv, b + 1u - (1u << k)));
 }
 
+// inner node c, whose range crosses a segment border
 template <typename Key>
-__global__ void __launch_bounds__(256)
-k_refit_ext(const Key *__restrict__ codes, uint32_t n, NodeRec *__restrict__ nodes,
-            const uint32_t *__restrict__ parents, TriRec *__restrict__ tris, const float *__restrict__ pre,
-            const float *__restrict__ suf, const float *__restrict__ t1, uint32_t nseg,
-            const float *__restrict__ t2, uint32_t ngrp, uint32_t *__restrict__ flags)
+__device__ __forceinline__ void refit_cross(const Key *__restrict__ codes, uint32_t n, uint32_t c,
+                                            NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
+                                            TriRec *__restrict__ tris, const float *__restrict__ pre,
+                                            const float *__restrict__ suf, const float *__restrict__ t1,
+                                            uint32_t nseg, const float *__restrict__ t2, uint32_t ngrp,
+                                            uint32_t *__restrict__ flags)
 {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c == 0u || c + 1u >= n) return;   // the root record is k_refit_top's
     uint32_t l, r;
-    if (!node_range(nodes[c].q3, n, l, r)) return;   // flagged by k_refit_seg
+    if (c + 1u >= n || !node_range(nodes[c].q3, n, l, r)) return;
     const uint32_t sa = l / kRefitSeg, sb = r / kRefitSeg;
-    if (sa == sb) return;   // k_refit_seg's
+    if (sa == sb) return;
     Box6 x = gload(suf, l);
     if (sa + 1u < sb) {
         // segment unions sa + 1 .. sb - 1, in 256-entry groups
@@ -498,6 +508,19 @@ k_refit_ext(const Key *__restrict__ codes, uint32_t n, NodeRec *__restrict__ nod
     }
     x = box_join(x, gload(pre, r));
     place_node(codes, n, c, l, r, x, nodes, parents, tris, flags);
+}
+
+template <typename Key>
+__global__ void __launch_bounds__(256)
+k_refit_ext(const Key *__restrict__ codes, uint32_t n, NodeRec *__restrict__ nodes,
+            const uint32_t *__restrict__ parents, TriRec *__restrict__ tris, const float *__restrict__ pre,
+            const float *__restrict__ suf, const float *__restrict__ t1, uint32_t nseg,
+            const float *__restrict__ t2, uint32_t ngrp, const uint32_t *__restrict__ cross,
+            const uint32_t *__restrict__ n_cross, uint32_t *__restrict__ flags)
+{
+    const uint32_t count = min(*n_cross, n);
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x)
+        refit_cross(codes, n, cross[e], nodes, parents, tris, pre, suf, t1, nseg, t2, ngrp, flags);
 }
 
 // ------------------------------------------------------------------------- //
@@ -577,7 +600,7 @@ struct rta_lbvh_ctx {
     NodeRec *nodes = nullptr;
     RootRec *root = nullptr;
     uint32_t *parents = nullptr;
-    uint32_t *counters = nullptr;
+    uint32_t *counters = nullptr;   // refit: the inner nodes that cross a segment border
     TriRec *tris = nullptr;
     uint32_t *status = nullptr;
     float *rbox = nullptr;   // refit tables: prefix and suffix unions, t1, t2
@@ -647,16 +670,19 @@ static int refit(rta_lbvh_ctx *c, uint32_t n, cudaStream_t s)
     const Key *codes = (const Key *)c->codes;
     float *pre = c->rbox + 6 * L.pre, *suf = c->rbox + 6 * L.suf;
     float *t1 = c->rbox + 6 * L.t1, *t2 = c->rbox + 6 * L.t2;
+    uint32_t *n_cross = &reinterpret_cast<SortScratchHeader *>(c->scratch)->n_cross;   // zeroed per build
     k_refit_seg<Key><<<L.nseg, kRefitSeg, 0, s>>>(codes, n, c->nodes, c->parents, c->tris, pre, suf, t1,
-                                                  c->status);
+                                                  c->counters, n_cross, c->status);
     int rc = check_launch("k_refit_seg");
     if (rc) return rc;
     k_refit_top<Key><<<L.ngrp, kRefitSeg, 0, s>>>(codes, n, t1, L.nseg, t2, L.ngrp, L.levels2, c->state, c->tris,
                                                   c->root);
     if ((rc = check_launch("k_refit_top"))) return rc;
     if (n > 2) {
-        k_refit_ext<Key><<<(n - 1 + 255) / 256, 256, 0, s>>>(codes, n, c->nodes, c->parents, c->tris, pre, suf,
-                                                             t1, L.nseg, t2, L.ngrp, c->status);
+        const uint32_t want = (n - 1 + 255) / 256, cap = (uint32_t)num_sms() * 4;
+        k_refit_ext<Key><<<want < cap ? want : cap, 256, 0, s>>>(codes, n, c->nodes, c->parents, c->tris, pre, suf,
+                                                                 t1, L.nseg, t2, L.ngrp, c->counters, n_cross,
+                                                                 c->status);
         if ((rc = check_launch("k_refit_ext"))) return rc;
     }
     return RTA_OK;

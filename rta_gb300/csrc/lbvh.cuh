@@ -34,6 +34,7 @@ struct BuildState {
 struct SortScratchHeader {
     uint32_t tile_ctr[kMaxPasses];
     uint32_t hist[kMaxPasses * kMaxRadix];
+    uint32_t n_cross;   // refit: inner nodes whose range crosses a segment border
 };
 
 // radix passes for `key_bits` bits at `digit_bits` per pass
