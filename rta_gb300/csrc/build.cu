@@ -378,7 +378,14 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n, NodeRec *__restrict__ nod
     const uint32_t t = threadIdx.x, base = blockIdx.x * kRefitSeg, j = base + t;
     const uint32_t cnt = min(kRefitSeg, n - base);
     Box6 b{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    if (j < n) b = leaf_box(tris[j]);
+    // this thread's loads are issued before the table build and land meanwhile
+    uint32_t leaf_pl = 0u;
+    uint4 q3 = make_uint4(0u, 0u, 0u, 0u);
+    if (j < n) {
+        b = leaf_box(tris[j]);
+        if (n > 1u) leaf_pl = parents[n - 1u + j];
+        if (j + 1u < n) q3 = nodes[j].q3;
+    }
     T.build(b);
     bool crosses = false;
     if (j < n) {
@@ -387,15 +394,14 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n, NodeRec *__restrict__ nod
         if (t == 0u) gstore(seg, blockIdx.x, T.query(0u, cnt - 1u));
         if (n > 1u) {
             // the leaf's box into its parent's record
-            const uint32_t pl = parents[n - 1u + j];
-            if ((pl >> 1) >= n - 1u) atomicOr(flags, RTA_DEV_BAD_LINK);
-            else write_slot(nodes + (pl >> 1), pl & 1u, b.lo, b.hi);
+            if ((leaf_pl >> 1) >= n - 1u) atomicOr(flags, RTA_DEV_BAD_LINK);
+            else write_slot(nodes + (leaf_pl >> 1), leaf_pl & 1u, b.lo, b.hi);
         }
         // inner node j (one end of its range): here when the range lies in this
         // segment, else on the list for k_refit_ext (the root is k_refit_top's)
         uint32_t l, r;
         if (j + 1u < n && j != 0u) {
-            if (!node_range(nodes[j].q3, n, l, r)) atomicOr(flags, RTA_DEV_BAD_LINK);
+            if (!node_range(q3, n, l, r)) atomicOr(flags, RTA_DEV_BAD_LINK);
             else if (l / kRefitSeg == r / kRefitSeg)
                 place_node(codes, n, j, l, r, T.query(l - base, r - base), nodes, parents, tris, flags);
             else crosses = true;

@@ -18,6 +18,12 @@ constexpr int kTriFloats = 26;         // cuda::simple_triangle = 104 bytes
 constexpr int kBoundsThreads = 256;
 constexpr int kSortThreads = 256;      // 8 warps
 constexpr int kSortItems = 16;
+// blocks per SM the onesweep kernel must fit in registers: 3 caps the 64-bit
+// key passes at 80 registers (from 128: 2 blocks per SM) at a few spilled
+// bytes, 1.5 % off the 4M build; 12 or 8 keys per thread measured slower
+#ifndef RTA_SORT_MIN_BLOCKS
+#define RTA_SORT_MIN_BLOCKS 3
+#endif
 constexpr int kSortTile = kSortThreads * kSortItems;   // 4096 keys per tile
 constexpr int kMaxDigitBits = 11;
 constexpr int kMaxRadix = 1 << kMaxDigitBits;
@@ -163,7 +169,7 @@ namespace {
 // key at its output position (the batched build's last pass writes the
 // per-mesh Morton codes this way).
 template <typename Key, int BITS>
-__global__ void __launch_bounds__(kSortThreads)
+__global__ void __launch_bounds__(kSortThreads, RTA_SORT_MIN_BLOCKS)
 k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *__restrict__ kout,
            uint32_t *__restrict__ vout, uint32_t n, int shift, uint32_t *__restrict__ tile_ctr,
            const uint32_t *__restrict__ hist, uint32_t *__restrict__ tstat, uint32_t *__restrict__ flags,
