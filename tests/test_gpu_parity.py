@@ -101,6 +101,22 @@ def test_build_matches_oracle(scene, bits):
                                   O.permute(tris, lb.ids).view(np.uint32))
 
 
+@pytest.mark.parametrize("n", [255, 256, 257, 511, 513, 65535, 65536, 65537, 70001])
+def test_build_at_refit_segment_and_group_borders(n):
+    """The refit unions boxes over 256-leaf segments and 256-segment groups:
+    triangle counts just below, at and above those borders (a last segment of
+    one leaf, a last group of one segment) give the oracle's tree.  Every
+    fourth triangle repeats its predecessor, so equal codes collapse across
+    the borders too."""
+    tris = S.clusters(1, n, seed=n)
+    tris[3::4, :9] = tris[2:-1:4, :9][: len(tris[3::4])]
+    for bits in (30, 63):
+        lb = O.lbvh_build(tris, bits)
+        bvh = gpu_build(tris, bits)
+        codes = lb.codes if bits == 63 else lb.codes.astype(np.uint32)
+        assert_build_equals(bvh, codes, lb.ids, lb.nodes)
+
+
 @pytest.mark.parametrize("digit_bits", [10, 11])
 @pytest.mark.parametrize("bits", [30, 63])
 def test_sort_digit_width_gives_the_same_tree(digit_bits, bits):
