@@ -11,7 +11,9 @@
 //            also writes each key's 30-bit code for the trees
 //   karras   every inner node of every mesh (its mesh is the key's top bits),
 //            Morton-ordered triangles, mesh-local ids
-//   refit    every leaf's climb inside its own mesh's tree
+//   refit    the range refit of lbvh.cuh over all meshes' leaves at once
+//            (a node's range never leaves its mesh; each mesh's root record
+//            takes its root's box)
 // and traced by one persistent launch over all rays (k_trace_batch in
 // trace.cu).  Because a stable sort by (mesh, code) orders each mesh's
 // triangles exactly as a sort by code alone does, and every per-mesh step
@@ -164,20 +166,6 @@ k_batch_karras(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ c
     ids[i] = lid;
 }
 
-__global__ void __launch_bounds__(256)
-k_batch_refit(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ codes, uint32_t n,
-              const MeshRec *__restrict__ meshes, NodeRec *__restrict__ nodes,
-              const uint32_t *__restrict__ parents, uint32_t *__restrict__ counters, TriRec *__restrict__ tris,
-              RootRec *__restrict__ roots, uint32_t *__restrict__ flags)
-{
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const uint32_t m = (uint32_t)(keys[j] >> 30);
-    const MeshRec mr = meshes[m];
-    refit_climb(codes + mr.tri_off, mr.n_tris, j - mr.tri_off, nodes + mr.node_off, parents + mr.parent_off,
-                counters + mr.node_off, tris + mr.tri_off, roots + m, flags);
-}
-
 // reset_intersections (librta/cuda-kernels.cu:24-44): t, beta, gamma; ref kept
 __global__ void k_batch_reset_hits(HitRec *__restrict__ hits, uint32_t n)
 {
@@ -227,9 +215,10 @@ struct rta_batch {
     unsigned char *scratch = nullptr;   // SortScratchHeader + tile status words
     NodeRec *nodes = nullptr;
     RootRec *roots = nullptr;
-    uint32_t *parents = nullptr, *counters = nullptr;
+    uint32_t *parents = nullptr, *counters = nullptr;   // counters: the refit's crossing-node list
     TriRec *tris = nullptr;
     uint32_t *status = nullptr;         // [0] flags, [4] trace queue
+    float *rbox = nullptr;              // refit tables (refit_layout)
     // result of the last build
     const uint64_t *keys_sorted = nullptr;
     uint32_t *index = nullptr;
@@ -246,7 +235,7 @@ static void free_batch(rta_batch *b)
 {
     void *ptrs[] = {b->meshes_d, b->tri_off_d, b->ray_off_d, b->box, b->cent, b->keys0, b->keys1,
                     b->vals0, b->vals1, b->codes, b->scratch, b->nodes, b->roots, b->parents,
-                    b->counters, b->tris, b->status};
+                    b->counters, b->tris, b->status, b->rbox};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -310,9 +299,11 @@ static int batch_build_impl(rta_batch *b, const void *tris, cudaStream_t s)
     k_batch_karras<<<eb, 256, 0, s>>>(ks, b->codes, vs, n, b->meshes_d, b->nodes, b->parents, b->counters, tin,
                                       b->tris);
     if ((rc = check_launch("k_batch_karras"))) return rc;
-    k_batch_refit<<<eb, 256, 0, s>>>(ks, b->codes, n, b->meshes_d, b->nodes, b->parents, b->counters, b->tris,
-                                     b->roots, b->status);
-    if ((rc = check_launch("k_batch_refit"))) return rc;
+    const uint32_t inner = n - b->meshes;
+    rc = refit_launch<uint32_t, true>(b->codes, n, b->meshes_d, ks, b->nodes, b->parents, b->tris, b->roots, b->rbox,
+                                      b->counters, inner ? inner : 1u, &hdr->n_cross, &hdr->refit_ticket, b->status,
+                                      batch_sms(), s);
+    if (rc) return rc;
     b->built = true;
     return RTA_OK;
 }
@@ -427,6 +418,7 @@ int rta_batch_set_meshes(rta_batch *b, uint32_t meshes, const uint32_t *tri_offs
     RTA_CUDA_TRY(cudaMalloc(&b->roots, (size_t)meshes * sizeof(RootRec)));
     RTA_CUDA_TRY(cudaMalloc(&b->parents, (2 * (size_t)nn - meshes) * 4));
     RTA_CUDA_TRY(cudaMalloc(&b->counters, (inner ? inner : 1) * 4));
+    RTA_CUDA_TRY(cudaMalloc(&b->rbox, refit_layout(nn).total * 6 * sizeof(float)));
     RTA_CUDA_TRY(cudaMalloc(&b->tris, (size_t)nn * sizeof(TriRec)));
     RTA_CUDA_TRY(cudaMalloc(&b->status, 64));
     RTA_CUDA_TRY(cudaMemset(b->status, 0, 64));

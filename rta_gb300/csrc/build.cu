@@ -209,327 +209,6 @@ k_karras(const Key *__restrict__ codes, const uint32_t *__restrict__ ids, uint32
 }
 
 // ------------------------------------------------------------------------- //
-// kernel: bottom-up refit                                                     //
-// ------------------------------------------------------------------------- //
-
-// ------------------------------------------------------------------------- //
-// kernels: refit over Morton ranges                                          //
-// ------------------------------------------------------------------------- //
-//
-// A node's box is the union of the leaf boxes over its Morton range [l, r],
-// so every node's box is a range query over the sorted leaves; no climb, no
-// arrival counters, no chain of dependent memory accesses.  The union is the
-// reference's (lbvh-kernels.cu:305-312) with the right child arriving
-// second: min = R < L ? R : L, max = R > L ? R : L, i.e. of equal values the
-// left one is kept.  Over a range that keeps the leftmost leaf among those
-// attaining the min (max) -- an associative rule, so any split of the range
-// (overlapping windows included) gives the value the sequential climb of the
-// CPU restatement gives.  (Only NaN coordinates make the result depend on
-// the grouping; the reference GPU climb is arrival-order dependent there.)
-//
-// The equal-code collapse (:300-331) makes a node a leaf exactly when all
-// codes of its range are equal (codes[l] == codes[r], the codes are sorted):
-// its link in the parent record becomes (first l, count r - l + 1), and the
-// triangle record at l keeps the count of the largest collapsed node that
-// starts there (atomic max; the climb writes the counts bottom-up).
-//
-// Three launches:
-//   k_refit_seg  one block per 256-leaf segment: a shared-memory sparse table
-//                of the leaf boxes; writes each leaf's box and the box of each
-//                inner node whose range lies in the segment into the parent
-//                record, plus per-leaf prefix / suffix unions and the segment
-//                union;
-//   k_refit_top  the same tables over the segment unions (256 segments per
-//                block), and in the last block a full sparse table over the
-//                block unions and the root record;
-//   k_refit_ext  the inner nodes whose range crosses a segment border: suffix
-//                of the first segment + segment unions between + prefix of
-//                the last segment.
-constexpr uint32_t kRefitSeg = 256;   // leaves per segment = threads per block
-constexpr int kRefitLevels = 8;       // sparse table levels 0..7 (windows of 1..128)
-
-struct Box6 {
-    float lo[3], hi[3];
-};
-
-__device__ __forceinline__ Box6 box_join(const Box6 &L, const Box6 &R)
-{
-    Box6 o;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        o.lo[k] = ref_min(R.lo[k], L.lo[k]);
-        o.hi[k] = ref_max(R.hi[k], L.hi[k]);
-    }
-    return o;
-}
-
-__device__ __forceinline__ Box6 leaf_box(const TriRec &t)
-{
-    const float a[3] = {t.v0.x, t.v0.y, t.v0.z}, b[3] = {t.v1.x, t.v1.y, t.v1.z}, c[3] = {t.v2.x, t.v2.y, t.v2.z};
-    Box6 o;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        o.lo[k] = ref_min(ref_min(a[k], b[k]), c[k]);
-        o.hi[k] = ref_max(ref_max(a[k], b[k]), c[k]);
-    }
-    return o;
-}
-
-// boxes in global memory: 24 bytes, (lo.x, lo.y) (lo.z, hi.x) (hi.y, hi.z)
-__device__ __forceinline__ Box6 gload(const float *base, size_t i)
-{
-    const float2 *p = reinterpret_cast<const float2 *>(base + 6 * i);
-    const float2 a = p[0], b = p[1], c = p[2];
-    return Box6{{a.x, a.y, b.x}, {b.y, c.x, c.y}};
-}
-__device__ __forceinline__ Box6 gload_cg(const float *base, size_t i)
-{
-    const float2 *p = reinterpret_cast<const float2 *>(base + 6 * i);
-    const float2 a = __ldcg(p), b = __ldcg(p + 1), c = __ldcg(p + 2);
-    return Box6{{a.x, a.y, b.x}, {b.y, c.x, c.y}};
-}
-__device__ __forceinline__ void gstore(float *base, size_t i, const Box6 &x)
-{
-    float2 *p = reinterpret_cast<float2 *>(base + 6 * i);
-    p[0] = make_float2(x.lo[0], x.lo[1]);
-    p[1] = make_float2(x.lo[2], x.hi[0]);
-    p[2] = make_float2(x.hi[1], x.hi[2]);
-}
-
-__device__ __forceinline__ int floor_log2(uint32_t v) { return 31 - __clz(v); }
-
-// the sparse table of one segment in shared memory: level k, component c, entry i
-struct SegTable {
-    float (*t)[6][kRefitSeg];
-    __device__ __forceinline__ Box6 get(int k, uint32_t i) const
-    {
-        return Box6{{t[k][0][i], t[k][1][i], t[k][2][i]}, {t[k][3][i], t[k][4][i], t[k][5][i]}};
-    }
-    __device__ __forceinline__ void put(int k, uint32_t i, const Box6 &x)
-    {
-        t[k][0][i] = x.lo[0]; t[k][1][i] = x.lo[1]; t[k][2][i] = x.lo[2];
-        t[k][3][i] = x.hi[0]; t[k][4][i] = x.hi[1]; t[k][5][i] = x.hi[2];
-    }
-    // union over entries [a, b] of the segment (two overlapping windows)
-    __device__ __forceinline__ Box6 query(uint32_t a, uint32_t b) const
-    {
-        const int k = min(floor_log2(b - a + 1u), kRefitLevels - 1);
-        return box_join(get(k, a), get(k, b + 1u - (1u << k)));
-    }
-    // level 0 holds one box per thread; levels 1..7 follow
-    __device__ __forceinline__ void build(const Box6 &x)
-    {
-        const uint32_t t_ = threadIdx.x;
-        put(0, t_, x);
-        __syncthreads();
-#pragma unroll 1
-        for (int k = 1; k < kRefitLevels; ++k) {
-            const uint32_t half = 1u << (k - 1);
-            Box6 y = get(k - 1, t_);
-            if (t_ + half < kRefitSeg) y = box_join(y, get(k - 1, t_ + half));
-            put(k, t_, y);
-            __syncthreads();
-        }
-    }
-};
-
-// Morton range [l, r] of inner node c from its record: the right child's
-// index, or its leaf's (or collapsed leaf's) first triangle, is split + 1
-// whichever of the three the record holds, and the sizes give the ends.
-__device__ __forceinline__ bool node_range(const uint4 q3, uint32_t n, uint32_t &l, uint32_t &r)
-{
-    const uint32_t rf = is_leaf(q3.y) ? leaf_first(q3.y) : q3.y;   // split + 1
-    const uint32_t ls = q3.z, rs = q3.w;
-    if (rf == 0u || ls == 0u || rs == 0u || ls > rf || rs > n - rf) return false;
-    l = rf - ls;
-    r = rf + rs - 1u;
-    return true;
-}
-
-// node c (not the root) with range [l, r] and box x into its parent's record
-template <typename Key>
-__device__ __forceinline__ void place_node(const Key *__restrict__ codes, uint32_t n, uint32_t c, uint32_t l,
-                                           uint32_t r, const Box6 &x, NodeRec *__restrict__ nodes,
-                                           const uint32_t *__restrict__ parents, TriRec *__restrict__ tris,
-                                           uint32_t *__restrict__ flags)
-{
-    const uint32_t pl = parents[c], p = pl >> 1, side = pl & 1u;
-    if (p >= n - 1u) {
-        atomicOr(flags, RTA_DEV_BAD_LINK);
-        return;
-    }
-    write_slot(nodes + p, side, x.lo, x.hi);
-    if (codes[l] == codes[r]) {   // collapsed: a leaf of r - l + 1 triangles
-        const uint32_t cnt = r - l + 1u;
-        reinterpret_cast<uint32_t *>(&nodes[p].q3)[side] = make_leaf(l, cnt);
-        atomicMax(reinterpret_cast<uint32_t *>(&tris[l].v0.w), cnt);
-    }
-}
-
-template <typename Key>
-__global__ void __launch_bounds__(kRefitSeg)
-k_refit_seg(const Key *__restrict__ codes, uint32_t n, NodeRec *__restrict__ nodes,
-            const uint32_t *__restrict__ parents, TriRec *__restrict__ tris, float *__restrict__ pre,
-            float *__restrict__ suf, float *__restrict__ seg, uint32_t *__restrict__ cross,
-            uint32_t *__restrict__ n_cross, uint32_t *__restrict__ flags)
-{
-    __shared__ float s_t[kRefitLevels][6][kRefitSeg];
-    SegTable T{s_t};
-    const uint32_t t = threadIdx.x, base = blockIdx.x * kRefitSeg, j = base + t;
-    const uint32_t cnt = min(kRefitSeg, n - base);
-    Box6 b{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    // this thread's loads are issued before the table build and land meanwhile
-    uint32_t leaf_pl = 0u;
-    uint4 q3 = make_uint4(0u, 0u, 0u, 0u);
-    if (j < n) {
-        b = leaf_box(tris[j]);
-        if (n > 1u) leaf_pl = parents[n - 1u + j];
-        if (j + 1u < n) q3 = nodes[j].q3;
-    }
-    T.build(b);
-    bool crosses = false;
-    if (j < n) {
-        gstore(pre, j, T.query(0u, t));
-        gstore(suf, j, T.query(t, cnt - 1u));
-        if (t == 0u) gstore(seg, blockIdx.x, T.query(0u, cnt - 1u));
-        if (n > 1u) {
-            // the leaf's box into its parent's record
-            if ((leaf_pl >> 1) >= n - 1u) atomicOr(flags, RTA_DEV_BAD_LINK);
-            else write_slot(nodes + (leaf_pl >> 1), leaf_pl & 1u, b.lo, b.hi);
-        }
-        // inner node j (one end of its range): here when the range lies in this
-        // segment, else on the list for k_refit_ext (the root is k_refit_top's)
-        uint32_t l, r;
-        if (j + 1u < n && j != 0u) {
-            if (!node_range(q3, n, l, r)) atomicOr(flags, RTA_DEV_BAD_LINK);
-            else if (l / kRefitSeg == r / kRefitSeg)
-                place_node(codes, n, j, l, r, T.query(l - base, r - base), nodes, parents, tris, flags);
-            else crosses = true;
-        }
-    }
-    const uint32_t lane = t & 31u, bm = __ballot_sync(0xffffffffu, crosses);
-    if (bm != 0u) {
-        const int leader = __ffs(bm) - 1;
-        uint32_t at = 0;
-        if ((int)lane == leader) at = atomicAdd(n_cross, (uint32_t)__popc(bm));
-        at = __shfl_sync(0xffffffffu, at, leader);
-        if (crosses) cross[at + __popc(bm & ((1u << lane) - 1u))] = j;
-    }
-}
-
-// Sparse tables over the segment unions: t1 level k entry i at t1 + 6 (k nseg
-// + i), built within 256-entry groups (level 0 = the segment unions); t2 the
-// full table over the group unions, level k entry i at t2 + 6 (k ngrp + i).
-template <typename Key>
-__global__ void __launch_bounds__(kRefitSeg)
-k_refit_top(const Key *__restrict__ codes, uint32_t n, float *__restrict__ t1, uint32_t nseg,
-            float *__restrict__ t2, uint32_t ngrp, int levels2, BuildState *__restrict__ st,
-            TriRec *__restrict__ tris, RootRec *__restrict__ root)
-{
-    __shared__ float s_t[kRefitLevels][6][kRefitSeg];
-    SegTable T{s_t};
-    const uint32_t t = threadIdx.x, base = blockIdx.x * kRefitSeg, i = base + t;
-    const uint32_t cnt = min(kRefitSeg, nseg - base);
-    Box6 b{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    if (i < nseg) b = gload(t1, i);
-    T.build(b);
-    if (i < nseg) {
-        for (int k = 1; k < kRefitLevels; ++k) gstore(t1, (size_t)k * nseg + i, T.get(k, t));
-    }
-    if (t == 0u) gstore(t2, blockIdx.x, T.query(0u, cnt - 1u));
-    // the last block to finish builds the table over the group unions
-    __threadfence();
-    bool last = false;
-    if (t == 0u) last = atomicAdd(&st->refit_done, 1u) == gridDim.x - 1u;
-    if (!__syncthreads_or(last)) return;
-    __threadfence();
-#pragma unroll 1
-    for (int k = 1; k < levels2; ++k) {
-        const uint32_t half = 1u << (k - 1);
-        for (uint32_t e = t; e < ngrp; e += kRefitSeg) {
-            const float *prev = t2 + 6 * (size_t)(k - 1) * ngrp;
-            Box6 y = gload_cg(prev, e);
-            if (e + half < ngrp) y = box_join(y, gload_cg(prev, e + half));
-            gstore(t2 + 6 * (size_t)k * ngrp, e, y);
-        }
-        __threadfence();
-        __syncthreads();
-    }
-    if (t == 0u) {
-        const int k = floor_log2(ngrp);
-        const float *lv = t2 + 6 * (size_t)k * ngrp;
-        const Box6 x = box_join(gload_cg(lv, 0), gload_cg(lv, ngrp - (1u << k)));
-        for (int a = 0; a < 3; ++a) {
-            root->lo[a] = x.lo[a];
-            root->hi[a] = x.hi[a];
-        }
-        if (n == 1u) {
-            root->link = make_leaf(0u, 1u);
-        } else if (codes[0] == codes[n - 1u]) {
-            root->link = make_leaf(0u, n);
-            atomicMax(reinterpret_cast<uint32_t *>(&tris[0].v0.w), n);
-        } else {
-            root->link = 0u;
-        }
-        st->refit_done = 0u;
-    }
-}
-
-__device__ __forceinline__ Box6 t1_query(const float *t1, uint32_t nseg, uint32_t a, uint32_t b)
-{
-    const int k = min(floor_log2(b - a + 1u), kRefitLevels - 1);
-    const float *lv = t1 + 6 * (size_t)k * nseg;
-    return box_join(gload(lv, a), gload(lv, b + 1u - (1u << k)));
-}
-
-// inner node c, whose range crosses a segment border
-template <typename Key>
-__device__ __forceinline__ void refit_cross(const Key *__restrict__ codes, uint32_t n, uint32_t c,
-                                            NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
-                                            TriRec *__restrict__ tris, const float *__restrict__ pre,
-                                            const float *__restrict__ suf, const float *__restrict__ t1,
-                                            uint32_t nseg, const float *__restrict__ t2, uint32_t ngrp,
-                                            uint32_t *__restrict__ flags)
-{
-    uint32_t l, r;
-    if (c + 1u >= n || !node_range(nodes[c].q3, n, l, r)) return;
-    const uint32_t sa = l / kRefitSeg, sb = r / kRefitSeg;
-    if (sa == sb) return;
-    Box6 x = gload(suf, l);
-    if (sa + 1u < sb) {
-        // segment unions sa + 1 .. sb - 1, in 256-entry groups
-        const uint32_t A = sa + 1u, B = sb - 1u, ga = A / kRefitSeg, gb = B / kRefitSeg;
-        if (ga == gb) {
-            x = box_join(x, t1_query(t1, nseg, A, B));
-        } else {
-            x = box_join(x, t1_query(t1, nseg, A, ga * kRefitSeg + kRefitSeg - 1u));
-            if (ga + 1u < gb) {
-                const uint32_t a2 = ga + 1u, b2 = gb - 1u;
-                const int k = floor_log2(b2 - a2 + 1u);
-                const float *lv = t2 + 6 * (size_t)k * ngrp;
-                x = box_join(x, box_join(gload(lv, a2), gload(lv, b2 + 1u - (1u << k))));
-            }
-            x = box_join(x, t1_query(t1, nseg, gb * kRefitSeg, B));
-        }
-    }
-    x = box_join(x, gload(pre, r));
-    place_node(codes, n, c, l, r, x, nodes, parents, tris, flags);
-}
-
-template <typename Key>
-__global__ void __launch_bounds__(256)
-k_refit_ext(const Key *__restrict__ codes, uint32_t n, NodeRec *__restrict__ nodes,
-            const uint32_t *__restrict__ parents, TriRec *__restrict__ tris, const float *__restrict__ pre,
-            const float *__restrict__ suf, const float *__restrict__ t1, uint32_t nseg,
-            const float *__restrict__ t2, uint32_t ngrp, const uint32_t *__restrict__ cross,
-            const uint32_t *__restrict__ n_cross, uint32_t *__restrict__ flags)
-{
-    const uint32_t count = min(*n_cross, n);
-    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x)
-        refit_cross(codes, n, cross[e], nodes, parents, tris, pre, suf, t1, nseg, t2, ngrp, flags);
-}
-
-// ------------------------------------------------------------------------- //
 // kernel: write the reference 2F4 node array (dumps and parity checks)       //
 // ------------------------------------------------------------------------- //
 
@@ -626,26 +305,6 @@ static int bounds_blocks(uint32_t n)
 
 static bool valid_digit_bits(int b) { return b == 8 || b == 10 || b == 11; }
 
-// sizes of the refit tables for n triangles (in boxes of 6 floats)
-struct RefitLayout {
-    uint32_t nseg, ngrp;
-    int levels2;
-    size_t pre, suf, t1, t2, total;
-};
-static RefitLayout refit_layout(uint32_t n)
-{
-    RefitLayout L;
-    L.nseg = (n + kRefitSeg - 1) / kRefitSeg;
-    L.ngrp = (L.nseg + kRefitSeg - 1) / kRefitSeg;
-    L.levels2 = 1;
-    while ((2u << (L.levels2 - 1)) <= L.ngrp) ++L.levels2;
-    L.pre = 0;
-    L.suf = L.pre + n;
-    L.t1 = L.suf + n;
-    L.t2 = L.t1 + (size_t)kRefitLevels * L.nseg;
-    L.total = L.t2 + (size_t)L.levels2 * L.ngrp;
-    return L;
-}
 
 // tile status words per tile, the most any supported digit width needs
 static size_t status_words_per_tile(int key_bits)
@@ -667,31 +326,6 @@ static void free_ctx(rta_lbvh_ctx *c)
     const int db = c->digit_bits;
     *c = rta_lbvh_ctx();
     c->digit_bits = db;
-}
-
-template <typename Key>
-static int refit(rta_lbvh_ctx *c, uint32_t n, cudaStream_t s)
-{
-    const RefitLayout L = refit_layout(n);
-    const Key *codes = (const Key *)c->codes;
-    float *pre = c->rbox + 6 * L.pre, *suf = c->rbox + 6 * L.suf;
-    float *t1 = c->rbox + 6 * L.t1, *t2 = c->rbox + 6 * L.t2;
-    uint32_t *n_cross = &reinterpret_cast<SortScratchHeader *>(c->scratch)->n_cross;   // zeroed per build
-    k_refit_seg<Key><<<L.nseg, kRefitSeg, 0, s>>>(codes, n, c->nodes, c->parents, c->tris, pre, suf, t1,
-                                                  c->counters, n_cross, c->status);
-    int rc = check_launch("k_refit_seg");
-    if (rc) return rc;
-    k_refit_top<Key><<<L.ngrp, kRefitSeg, 0, s>>>(codes, n, t1, L.nseg, t2, L.ngrp, L.levels2, c->state, c->tris,
-                                                  c->root);
-    if ((rc = check_launch("k_refit_top"))) return rc;
-    if (n > 2) {
-        const uint32_t want = (n - 1 + 255) / 256, cap = (uint32_t)num_sms() * 4;
-        k_refit_ext<Key><<<want < cap ? want : cap, 256, 0, s>>>(codes, n, c->nodes, c->parents, c->tris, pre, suf,
-                                                                 t1, L.nseg, t2, L.ngrp, c->counters, n_cross,
-                                                                 c->status);
-        if ((rc = check_launch("k_refit_ext"))) return rc;
-    }
-    return RTA_OK;
 }
 
 template <typename Key>
@@ -831,7 +465,13 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
                                               c->parents, c->counters, tin, c->tris,
                                               (float *)tris_out);
     if ((rc = check_launch("k_karras"))) return rc;
-    rc = bits == 63 ? refit<uint64_t>(c, n, s) : refit<uint32_t>(c, n, s);
+    const uint32_t cap = n > 1 ? n - 1 : 1;
+    rc = bits == 63 ? refit_launch<uint64_t, false>((const uint64_t *)c->codes, n, nullptr, nullptr, c->nodes,
+                                                    c->parents, c->tris, c->root, c->rbox, c->counters, cap,
+                                                    &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s)
+                    : refit_launch<uint32_t, false>((const uint32_t *)c->codes, n, nullptr, nullptr, c->nodes,
+                                                    c->parents, c->tris, c->root, c->rbox, c->counters, cap,
+                                                    &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s);
     if (rc) return rc;
     c->n = n;
     c->last_bits = bits;

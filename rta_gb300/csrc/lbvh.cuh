@@ -1,11 +1,12 @@
 // lbvh.cuh -- device pieces of the LBVH build shared by the one-mesh builder
 // (build.cu) and the batched multi-mesh builder (batch.cu): build constants,
 // position loads, Morton helpers, the onesweep radix pass, Karras' split
-// search, the per-node link writer and the bottom-up refit climb.
+// search, the per-node link writer and the refit over Morton ranges.
 #pragma once
 
 #include <utility>
 
+#include "batch.cuh"
 #include "common.cuh"
 
 namespace rta {
@@ -32,7 +33,6 @@ constexpr int kMaxPasses = 8;          // 63-bit keys at 8 bits per digit
 struct BuildState {
     float lo[3], hi[3], scale[3];
     uint32_t done;                 // bounds last-block ticket (self-resetting)
-    uint32_t refit_done;           // refit summary last-block ticket (self-resetting)
 };
 
 // Zeroed by one memset before every build.  hist holds the global digit
@@ -40,7 +40,8 @@ struct BuildState {
 struct SortScratchHeader {
     uint32_t tile_ctr[kMaxPasses];
     uint32_t hist[kMaxPasses * kMaxRadix];
-    uint32_t n_cross;   // refit: inner nodes whose range crosses a segment border
+    uint32_t n_cross;        // refit: inner nodes whose range crosses a segment border
+    uint32_t refit_ticket;   // refit: last-block ticket of k_refit_top
 };
 
 // radix passes for `key_bits` bits at `digit_bits` per pass
@@ -412,14 +413,40 @@ __device__ __forceinline__ TriRec make_tri(const float *__restrict__ src, uint32
 }
 
 // ------------------------------------------------------------------------- //
-// bottom-up refit                                                             //
+// refit over Morton ranges                                                    //
 // ------------------------------------------------------------------------- //
 //
-// One thread per leaf climbs towards the root; the second thread to arrive at
-// a node (counted with an acquire-release atomic add)
-// unions the two child boxes, applies the reference's collapse rule (both
-// children leaves with equal Morton codes -> one multi-triangle leaf,
-// :300-331) and continues.  A node's box is stored in its parent's record.
+// A node's box is the union of the leaf boxes over its Morton range [l, r],
+// so every node's box is a range query over the sorted leaves: no climb, no
+// arrival counters, no chain of dependent memory accesses.  The union is the
+// reference's (lbvh-kernels.cu:305-312) with the right child arriving
+// second: min = R < L ? R : L, max = R > L ? R : L, i.e. of equal values the
+// left one is kept.  Over a range that keeps the leftmost leaf among those
+// attaining the min (max) -- an associative rule, so any split of the range
+// (overlapping windows included) gives the bits of the CPU restatement's
+// sequential climb.  (Only NaN coordinates make the result depend on the
+// grouping; the reference GPU climb is arrival-order dependent there.)
+//
+// The equal-code collapse (:300-331) makes a node a leaf exactly when all
+// codes of its range are equal (codes[l] == codes[r], the codes are sorted):
+// its link in the parent record becomes (first l, count r - l + 1), and the
+// triangle record at l keeps the count of the largest collapsed node that
+// starts there (atomic max; a climb writes the counts bottom-up).
+//
+// The leaves of all meshes of a batch are one sorted sequence (a mesh's
+// leaves are contiguous), and a node's range never leaves its mesh, so the
+// segment tables below are built across mesh borders and the queries stay
+// exact.  Three launches:
+//   k_refit_seg  one block per 256-leaf segment: a shared-memory sparse table
+//                of the leaf boxes; writes each leaf's box and the box of each
+//                inner node whose range lies in the segment into the parent
+//                record (a mesh's root into its root record), per-leaf prefix
+//                / suffix unions and the segment union, and lists the inner
+//                nodes whose range crosses a segment border;
+//   k_refit_top  the same tables over the segment unions in 256-entry groups,
+//                and in the last block a full sparse table over the groups;
+//   k_refit_ext  each listed node: suffix of its first segment + segment
+//                unions between + prefix of its last segment.
 
 __device__ __forceinline__ void write_slot(NodeRec *nd, uint32_t side, const float lo[3],
                                            const float hi[3])
@@ -432,110 +459,369 @@ __device__ __forceinline__ void write_slot(NodeRec *nd, uint32_t side, const flo
     }
 }
 
-__device__ __forceinline__ void read_slot_cg(const NodeRec *nd, uint32_t side, float lo[3], float hi[3])
+constexpr uint32_t kRefitSeg = 256;   // leaves per segment = threads per block
+constexpr int kRefitLevels = 8;       // sparse table levels 0..7 (windows of 1..128)
+
+struct Box6 {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ Box6 box_join(const Box6 &L, const Box6 &R)
 {
-    const float *f = reinterpret_cast<const float *>(nd);
+    Box6 o;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        lo[k] = __ldcg(f + slot_lo(side, k));
-        hi[k] = __ldcg(f + slot_hi(side, k));
+        o.lo[k] = ref_min(R.lo[k], L.lo[k]);
+        o.hi[k] = ref_max(R.hi[k], L.hi[k]);
     }
+    return o;
 }
 
-// Arrival count with acquire-release semantics at device scope: the first
-// arriver's box and link writes (program-ordered before it) are released by
-// it, and the second arriver acquires them before it reads the sibling slot.
-// One instruction instead of a fence on both sides of a relaxed atomicAdd.
-__device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t *p)
+__device__ __forceinline__ Box6 leaf_box(const TriRec &t)
 {
-    uint32_t old;
-    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
-    return old;
-}
-
-__device__ __forceinline__ uint32_t leaf_count_cg(uint32_t link, const TriRec *tris)
-{
-    uint32_t f = leaf_count_field(link);
-    if (f < 63u) return f + 1u;
-    return __float_as_uint(__ldcg(&tris[leaf_first(link)].v0.w));
-}
-
-// the climb of leaf j of a tree over codes[0, n)
-template <typename Key>
-__device__ __forceinline__ void refit_climb(const Key *__restrict__ codes, uint32_t n, uint32_t j,
-                                            NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
-                                            uint32_t *__restrict__ counters, TriRec *__restrict__ tris,
-                                            RootRec *__restrict__ root, uint32_t *__restrict__ flags)
-{
-    float lo[3], hi[3];
-    {
-        TriRec t = tris[j];
-        const float a[3] = {t.v0.x, t.v0.y, t.v0.z};
-        const float b[3] = {t.v1.x, t.v1.y, t.v1.z};
-        const float c[3] = {t.v2.x, t.v2.y, t.v2.z};
+    const float a[3] = {t.v0.x, t.v0.y, t.v0.z}, b[3] = {t.v1.x, t.v1.y, t.v1.z}, c[3] = {t.v2.x, t.v2.y, t.v2.z};
+    Box6 o;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            lo[k] = ref_min(ref_min(a[k], b[k]), c[k]);
-            hi[k] = ref_max(ref_max(a[k], b[k]), c[k]);
+    for (int k = 0; k < 3; ++k) {
+        o.lo[k] = ref_min(ref_min(a[k], b[k]), c[k]);
+        o.hi[k] = ref_max(ref_max(a[k], b[k]), c[k]);
+    }
+    return o;
+}
+
+// boxes in global memory: 24 bytes, (lo.x, lo.y) (lo.z, hi.x) (hi.y, hi.z)
+__device__ __forceinline__ Box6 gload(const float *base, size_t i)
+{
+    const float2 *p = reinterpret_cast<const float2 *>(base + 6 * i);
+    const float2 a = p[0], b = p[1], c = p[2];
+    return Box6{{a.x, a.y, b.x}, {b.y, c.x, c.y}};
+}
+__device__ __forceinline__ Box6 gload_cg(const float *base, size_t i)
+{
+    const float2 *p = reinterpret_cast<const float2 *>(base + 6 * i);
+    const float2 a = __ldcg(p), b = __ldcg(p + 1), c = __ldcg(p + 2);
+    return Box6{{a.x, a.y, b.x}, {b.y, c.x, c.y}};
+}
+__device__ __forceinline__ void gstore(float *base, size_t i, const Box6 &x)
+{
+    float2 *p = reinterpret_cast<float2 *>(base + 6 * i);
+    p[0] = make_float2(x.lo[0], x.lo[1]);
+    p[1] = make_float2(x.lo[2], x.hi[0]);
+    p[2] = make_float2(x.hi[1], x.hi[2]);
+}
+
+__device__ __forceinline__ int floor_log2(uint32_t v) { return 31 - __clz(v); }
+
+// the sparse table of one segment in shared memory: level k, component c, entry i
+struct SegTable {
+    float (*t)[6][kRefitSeg];
+    __device__ __forceinline__ Box6 get(int k, uint32_t i) const
+    {
+        return Box6{{t[k][0][i], t[k][1][i], t[k][2][i]}, {t[k][3][i], t[k][4][i], t[k][5][i]}};
+    }
+    __device__ __forceinline__ void put(int k, uint32_t i, const Box6 &x)
+    {
+        t[k][0][i] = x.lo[0]; t[k][1][i] = x.lo[1]; t[k][2][i] = x.lo[2];
+        t[k][3][i] = x.hi[0]; t[k][4][i] = x.hi[1]; t[k][5][i] = x.hi[2];
+    }
+    // union over entries [a, b] of the segment (two overlapping windows)
+    __device__ __forceinline__ Box6 query(uint32_t a, uint32_t b) const
+    {
+        const int k = min(floor_log2(b - a + 1u), kRefitLevels - 1);
+        return box_join(get(k, a), get(k, b + 1u - (1u << k)));
+    }
+    // level 0 holds one box per thread; levels 1..7 follow
+    __device__ __forceinline__ void build(const Box6 &x)
+    {
+        const uint32_t t_ = threadIdx.x;
+        put(0, t_, x);
+        __syncthreads();
+#pragma unroll 1
+        for (int k = 1; k < kRefitLevels; ++k) {
+            const uint32_t half = 1u << (k - 1);
+            Box6 y = get(k - 1, t_);
+            if (t_ + half < kRefitSeg) y = box_join(y, get(k - 1, t_ + half));
+            put(k, t_, y);
+            __syncthreads();
         }
     }
-    uint32_t link = make_leaf(j, 1u);   // link of the current node, as its parent stores it
-    bool link_changed = false;
-    Key code = codes[j];
-    uint32_t cur = n - 1 + j;
-    if (n == 1) {
-        for (int k = 0; k < 3; ++k) { root->lo[k] = lo[k]; root->hi[k] = hi[k]; }
-        root->link = link;
+};
+
+__device__ __forceinline__ Box6 t1_query(const float *t1, uint32_t nseg, uint32_t a, uint32_t b)
+{
+    const int k = min(floor_log2(b - a + 1u), kRefitLevels - 1);
+    const float *lv = t1 + 6 * (size_t)k * nseg;
+    return box_join(gload(lv, a), gload(lv, b + 1u - (1u << k)));
+}
+
+// Morton range [l, r] (local to its mesh) of an inner node from its record:
+// the right child's index, or its leaf's (or collapsed leaf's) first
+// triangle, is split + 1 whichever of the three the record holds, and the
+// subtree sizes give the ends.
+__device__ __forceinline__ bool node_range(const uint4 q3, uint32_t n, uint32_t &l, uint32_t &r)
+{
+    const uint32_t rf = is_leaf(q3.y) ? leaf_first(q3.y) : q3.y;   // split + 1
+    const uint32_t ls = q3.z, rs = q3.w;
+    if (rf == 0u || ls == 0u || rs == 0u || ls > rf || rs > n - rf) return false;
+    l = rf - ls;
+    r = rf + rs - 1u;
+    return true;
+}
+
+// The mesh that leaf position j (global) belongs to.  One tree: the whole
+// range.  A batch: the mesh id is the sorted key's top bits.
+struct MeshSpan {
+    uint32_t m, tri_off, n, node_off, parent_off;
+};
+template <bool BATCH>
+__device__ __forceinline__ MeshSpan mesh_of(uint32_t j, uint32_t n_all, const MeshRec *__restrict__ meshes,
+                                            const uint64_t *__restrict__ keys)
+{
+    if (!BATCH) return MeshSpan{0u, 0u, n_all, 0u, 0u};
+    const uint32_t m = (uint32_t)(keys[j] >> 30);
+    const MeshRec mr = meshes[m];
+    return MeshSpan{m, mr.tri_off, mr.n_tris, mr.node_off, mr.parent_off};
+}
+
+// inner node c (local to mesh sp) with global range [gl, gr] and box x: into
+// its parent's record, or the mesh's root record for c = 0
+template <typename Key>
+__device__ __forceinline__ void place_node(const Key *__restrict__ codes, const MeshSpan &sp, uint32_t c,
+                                           uint32_t gl, uint32_t gr, const Box6 &x, NodeRec *__restrict__ nodes,
+                                           const uint32_t *__restrict__ parents, TriRec *__restrict__ tris,
+                                           RootRec *__restrict__ roots, uint32_t *__restrict__ flags)
+{
+    const bool collapsed = codes[gl] == codes[gr];   // a leaf of gr - gl + 1 triangles
+    const uint32_t cnt = gr - gl + 1u;
+    if (collapsed) atomicMax(reinterpret_cast<uint32_t *>(&tris[gl].v0.w), cnt);
+    if (c == 0u) {
+        RootRec &R = roots[sp.m];
+        for (int a = 0; a < 3; ++a) {
+            R.lo[a] = x.lo[a];
+            R.hi[a] = x.hi[a];
+        }
+        R.link = collapsed ? make_leaf(0u, cnt) : 0u;
         return;
     }
-    // a path to the root has at most 2 * (key bits + index bits) nodes
-    for (uint32_t climb = 0;; ++climb) {
-        if (climb > 256u) {
-            atomicOr(flags, RTA_DEV_ITER_LIMIT);
-            return;
-        }
-        const uint32_t pl = parents[cur];
-        const uint32_t p = pl >> 1, side = pl & 1u;
-        if (p >= n - 1) {
+    const uint32_t pl = parents[sp.parent_off + c], p = pl >> 1, side = pl & 1u;
+    if (p >= sp.n - 1u) {
+        atomicOr(flags, RTA_DEV_BAD_LINK);
+        return;
+    }
+    NodeRec *nd = nodes + sp.node_off + p;
+    write_slot(nd, side, x.lo, x.hi);
+    if (collapsed) reinterpret_cast<uint32_t *>(&nd->q3)[side] = make_leaf(gl - sp.tri_off, cnt);
+}
+
+namespace {
+
+template <typename Key, bool BATCH>
+__global__ void __launch_bounds__(kRefitSeg)
+k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__restrict__ meshes,
+            const uint64_t *__restrict__ keys, NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
+            TriRec *__restrict__ tris, RootRec *__restrict__ roots, float *__restrict__ pre,
+            float *__restrict__ suf, float *__restrict__ seg, uint32_t *__restrict__ cross,
+            uint32_t *__restrict__ n_cross, uint32_t *__restrict__ flags)
+{
+    __shared__ float s_t[kRefitLevels][6][kRefitSeg];
+    SegTable T{s_t};
+    const uint32_t t = threadIdx.x, base = blockIdx.x * kRefitSeg, j = base + t;
+    const uint32_t cnt = min(kRefitSeg, n_all - base);
+    Box6 b{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    // this thread's loads are issued before the table build and land meanwhile
+    MeshSpan sp{0u, 0u, 1u, 0u, 0u};
+    uint32_t leaf_pl = 0u, jl = 0u;
+    uint4 q3 = make_uint4(0u, 0u, 0u, 0u);
+    if (j < n_all) {
+        sp = mesh_of<BATCH>(j, n_all, meshes, keys);
+        jl = j - sp.tri_off;
+        b = leaf_box(tris[j]);
+        if (sp.n > 1u) leaf_pl = parents[sp.parent_off + sp.n - 1u + jl];
+        if (jl + 1u < sp.n) q3 = nodes[sp.node_off + jl].q3;
+    }
+    T.build(b);
+    bool crosses = false;
+    if (j < n_all) {
+        gstore(pre, j, T.query(0u, t));
+        gstore(suf, j, T.query(t, cnt - 1u));
+        if (t == 0u) gstore(seg, blockIdx.x, T.query(0u, cnt - 1u));
+        if (sp.n == 1u) {   // a one-triangle mesh: its root is the leaf
+            RootRec &R = roots[sp.m];
+            for (int a = 0; a < 3; ++a) {
+                R.lo[a] = b.lo[a];
+                R.hi[a] = b.hi[a];
+            }
+            R.link = make_leaf(0u, 1u);
+        } else if ((leaf_pl >> 1) >= sp.n - 1u) {
             atomicOr(flags, RTA_DEV_BAD_LINK);
-            return;
+        } else {   // the leaf's box into its parent's record
+            write_slot(nodes + sp.node_off + (leaf_pl >> 1), leaf_pl & 1u, b.lo, b.hi);
         }
-        NodeRec *nd = nodes + p;
-        write_slot(nd, side, lo, hi);
-        if (link_changed) reinterpret_cast<uint32_t *>(&nd->q3)[side] = link;
-        if (arrive_acq_rel(counters + p) == 0u) return;   // first arrival stops
-        float slo[3], shi[3];
-        read_slot_cg(nd, side ^ 1u, slo, shi);
-        const uint32_t sib = __ldcg(reinterpret_cast<const uint32_t *>(&nd->q3) + (side ^ 1u));
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            lo[k] = ref_min(lo[k], slo[k]);
-            hi[k] = ref_max(hi[k], shi[k]);
-        }
-        if ((is_leaf(sib) ? leaf_first(sib) : sib) >= n) {
-            atomicOr(flags, RTA_DEV_BAD_LINK);
-            return;
-        }
-        const Key sib_code = is_leaf(sib) ? codes[leaf_first(sib)] : codes[sib];
-        link_changed = false;
-        uint32_t plink = p;
-        if (code == sib_code && is_leaf(link) && is_leaf(sib)) {
-            const uint32_t f0 = leaf_first(link), f1 = leaf_first(sib);
-            const uint32_t cnt = leaf_count_cg(link, tris) + leaf_count_cg(sib, tris);
-            const uint32_t first = f0 < f1 ? f0 : f1;
-            tris[first].v0.w = __uint_as_float(cnt);
-            plink = make_leaf(first, cnt);
-            link_changed = true;
-        }
-        link = plink;
-        code = codes[p];
-        cur = p;
-        if (p == 0) {
-            for (int k = 0; k < 3; ++k) { root->lo[k] = lo[k]; root->hi[k] = hi[k]; }
-            root->link = link;
-            return;
+        // inner node jl of the mesh (one end of its range): here when the range
+        // lies in this segment, else on the list for k_refit_ext
+        uint32_t l, r;
+        if (jl + 1u < sp.n) {
+            if (!node_range(q3, sp.n, l, r)) {
+                atomicOr(flags, RTA_DEV_BAD_LINK);
+            } else {
+                const uint32_t gl = sp.tri_off + l, gr = sp.tri_off + r;
+                if (gl / kRefitSeg == gr / kRefitSeg)
+                    place_node(codes, sp, jl, gl, gr, T.query(gl - base, gr - base), nodes, parents, tris, roots,
+                               flags);
+                else
+                    crosses = true;
+            }
         }
     }
+    const uint32_t lane = t & 31u, bm = __ballot_sync(0xffffffffu, crosses);
+    if (bm != 0u) {
+        const int leader = __ffs(bm) - 1;
+        uint32_t at = 0;
+        if ((int)lane == leader) at = atomicAdd(n_cross, (uint32_t)__popc(bm));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (crosses) cross[at + __popc(bm & ((1u << lane) - 1u))] = j;
+    }
+}
+
+// Sparse tables over the segment unions: t1 level k entry i at t1 + 6 (k nseg
+// + i), built within 256-entry groups (level 0 = the segment unions); t2 the
+// full table over the group unions, level k entry i at t2 + 6 (k ngrp + i).
+__global__ void __launch_bounds__(kRefitSeg)
+k_refit_top(float *__restrict__ t1, uint32_t nseg, float *__restrict__ t2, uint32_t ngrp, int levels2,
+            uint32_t *__restrict__ ticket)
+{
+    __shared__ float s_t[kRefitLevels][6][kRefitSeg];
+    SegTable T{s_t};
+    const uint32_t t = threadIdx.x, base = blockIdx.x * kRefitSeg, i = base + t;
+    const uint32_t cnt = min(kRefitSeg, nseg - base);
+    Box6 b{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    if (i < nseg) b = gload(t1, i);
+    T.build(b);
+    if (i < nseg) {
+        for (int k = 1; k < kRefitLevels; ++k) gstore(t1, (size_t)k * nseg + i, T.get(k, t));
+    }
+    if (t == 0u) gstore(t2, blockIdx.x, T.query(0u, cnt - 1u));
+    // the last block to finish builds the table over the group unions
+    __threadfence();
+    bool last = false;
+    if (t == 0u) last = atomicAdd(ticket, 1u) == gridDim.x - 1u;
+    if (!__syncthreads_or(last)) return;
+    __threadfence();
+#pragma unroll 1
+    for (int k = 1; k < levels2; ++k) {
+        const uint32_t half = 1u << (k - 1);
+        const float *prev = t2 + 6 * (size_t)(k - 1) * ngrp;
+        for (uint32_t e = t; e < ngrp; e += kRefitSeg) {
+            Box6 y = gload_cg(prev, e);
+            if (e + half < ngrp) y = box_join(y, gload_cg(prev, e + half));
+            gstore(t2 + 6 * (size_t)k * ngrp, e, y);
+        }
+        __threadfence();
+        __syncthreads();
+    }
+}
+
+// the listed inner node at leaf position j, whose range crosses a segment border
+template <typename Key, bool BATCH>
+__device__ __forceinline__ void refit_cross(const Key *__restrict__ codes, uint32_t n_all, uint32_t j,
+                                            const MeshRec *__restrict__ meshes, const uint64_t *__restrict__ keys,
+                                            NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
+                                            TriRec *__restrict__ tris, RootRec *__restrict__ roots,
+                                            const float *__restrict__ pre, const float *__restrict__ suf,
+                                            const float *__restrict__ t1, uint32_t nseg, const float *__restrict__ t2,
+                                            uint32_t ngrp, uint32_t *__restrict__ flags)
+{
+    if (j >= n_all) return;
+    const MeshSpan sp = mesh_of<BATCH>(j, n_all, meshes, keys);
+    const uint32_t jl = j - sp.tri_off;
+    uint32_t l, r;
+    if (jl + 1u >= sp.n || !node_range(nodes[sp.node_off + jl].q3, sp.n, l, r)) return;
+    const uint32_t gl = sp.tri_off + l, gr = sp.tri_off + r;
+    const uint32_t sa = gl / kRefitSeg, sb = gr / kRefitSeg;
+    if (sa == sb) return;
+    Box6 x = gload(suf, gl);
+    if (sa + 1u < sb) {
+        // segment unions sa + 1 .. sb - 1, in 256-entry groups
+        const uint32_t A = sa + 1u, B = sb - 1u, ga = A / kRefitSeg, gb = B / kRefitSeg;
+        if (ga == gb) {
+            x = box_join(x, t1_query(t1, nseg, A, B));
+        } else {
+            x = box_join(x, t1_query(t1, nseg, A, ga * kRefitSeg + kRefitSeg - 1u));
+            if (ga + 1u < gb) {
+                const uint32_t a2 = ga + 1u, b2 = gb - 1u;
+                const int k = floor_log2(b2 - a2 + 1u);
+                const float *lv = t2 + 6 * (size_t)k * ngrp;
+                x = box_join(x, box_join(gload(lv, a2), gload(lv, b2 + 1u - (1u << k))));
+            }
+            x = box_join(x, t1_query(t1, nseg, gb * kRefitSeg, B));
+        }
+    }
+    x = box_join(x, gload(pre, gr));
+    place_node(codes, sp, jl, gl, gr, x, nodes, parents, tris, roots, flags);
+}
+
+template <typename Key, bool BATCH>
+__global__ void __launch_bounds__(256)
+k_refit_ext(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__restrict__ meshes,
+            const uint64_t *__restrict__ keys, NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
+            TriRec *__restrict__ tris, RootRec *__restrict__ roots, const float *__restrict__ pre,
+            const float *__restrict__ suf, const float *__restrict__ t1, uint32_t nseg,
+            const float *__restrict__ t2, uint32_t ngrp, const uint32_t *__restrict__ cross,
+            const uint32_t *__restrict__ n_cross, uint32_t cross_cap, uint32_t *__restrict__ flags)
+{
+    const uint32_t count = min(*n_cross, cross_cap);
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x)
+        refit_cross<Key, BATCH>(codes, n_all, cross[e], meshes, keys, nodes, parents, tris, roots, pre, suf, t1,
+                                nseg, t2, ngrp, flags);
+}
+
+} // namespace
+
+// sizes of the refit tables for n leaves (in boxes of 6 floats)
+struct RefitLayout {
+    uint32_t nseg, ngrp;
+    int levels2;
+    size_t pre, suf, t1, t2, total;
+};
+inline RefitLayout refit_layout(uint32_t n)
+{
+    RefitLayout L;
+    L.nseg = (n + kRefitSeg - 1) / kRefitSeg;
+    L.ngrp = (L.nseg + kRefitSeg - 1) / kRefitSeg;
+    L.levels2 = 1;
+    while ((2u << (L.levels2 - 1)) <= L.ngrp) ++L.levels2;
+    L.pre = 0;
+    L.suf = L.pre + n;
+    L.t1 = L.suf + n;
+    L.t2 = L.t1 + (size_t)kRefitLevels * L.nseg;
+    L.total = L.t2 + (size_t)L.levels2 * L.ngrp;
+    return L;
+}
+
+// The refit of n_all leaves after the Karras kernel: tables in rbox
+// (refit_layout(n_all).total boxes), the crossing list in cross (one word per
+// inner node: cross_cap), *n_cross and *ticket zero on entry.
+template <typename Key, bool BATCH>
+int refit_launch(const Key *codes, uint32_t n_all, const MeshRec *meshes, const uint64_t *keys, NodeRec *nodes,
+                 const uint32_t *parents, TriRec *tris, RootRec *roots, float *rbox, uint32_t *cross,
+                 uint32_t cross_cap, uint32_t *n_cross, uint32_t *ticket, uint32_t *flags, int sms, cudaStream_t s)
+{
+    const RefitLayout L = refit_layout(n_all);
+    float *pre = rbox + 6 * L.pre, *suf = rbox + 6 * L.suf, *t1 = rbox + 6 * L.t1, *t2 = rbox + 6 * L.t2;
+    k_refit_seg<Key, BATCH><<<L.nseg, kRefitSeg, 0, s>>>(codes, n_all, meshes, keys, nodes, parents, tris, roots,
+                                                         pre, suf, t1, cross, n_cross, flags);
+    int rc = check_launch("k_refit_seg");
+    if (rc) return rc;
+    k_refit_top<<<L.ngrp, kRefitSeg, 0, s>>>(t1, L.nseg, t2, L.ngrp, L.levels2, ticket);
+    if ((rc = check_launch("k_refit_top"))) return rc;
+    if (n_all > 2u) {
+        const uint32_t want = (n_all + 255u) / 256u, cap = (uint32_t)sms * 4u;
+        k_refit_ext<Key, BATCH><<<want < cap ? want : cap, 256, 0, s>>>(codes, n_all, meshes, keys, nodes, parents,
+                                                                        tris, roots, pre, suf, t1, L.nseg, t2,
+                                                                        L.ngrp, cross, n_cross, cross_cap, flags);
+        if ((rc = check_launch("k_refit_ext"))) return rc;
+    }
+    return RTA_OK;
 }
 
 } // namespace rta
