@@ -461,6 +461,9 @@ __device__ __forceinline__ void write_slot(NodeRec *nd, uint32_t side, const flo
 
 constexpr uint32_t kRefitSeg = 256;   // leaves per segment = threads per block
 constexpr int kRefitLevels = 8;       // sparse table levels 0..7 (windows of 1..128)
+// groups of 256 segments whose table k_refit_top builds in shared memory (2^25 leaves)
+constexpr uint32_t kMaxGroups = (kMaxTriangles + kRefitSeg * kRefitSeg - 1) / (kRefitSeg * kRefitSeg);
+static_assert(2 * 6 * kMaxGroups <= kRefitLevels * 6 * kRefitSeg, "group table fits the segment table space");
 
 struct Box6 {
     float lo[3], hi[3];
@@ -707,16 +710,48 @@ k_refit_top(float *__restrict__ t1, uint32_t nseg, float *__restrict__ t2, uint3
     if (t == 0u) last = atomicAdd(ticket, 1u) == gridDim.x - 1u;
     if (!__syncthreads_or(last)) return;
     __threadfence();
+    if (ngrp > kMaxGroups) {   // batches beyond 2^25 leaves: level by level through L2
+#pragma unroll 1
+        for (int k = 1; k < levels2; ++k) {
+            const uint32_t half = 1u << (k - 1);
+            const float *prev = t2 + 6 * (size_t)(k - 1) * ngrp;
+            for (uint32_t e = t; e < ngrp; e += kRefitSeg) {
+                Box6 y = gload_cg(prev, e);
+                if (e + half < ngrp) y = box_join(y, gload_cg(prev, e + half));
+                gstore(t2 + 6 * (size_t)k * ngrp, e, y);
+            }
+            __threadfence();
+            __syncthreads();
+        }
+        return;
+    }
+    // the group table in this block's shared memory (two levels of up to
+    // kMaxGroups entries in the segment table's space), each level stored out
+    float(*lv)[6][kMaxGroups] = reinterpret_cast<float(*)[6][kMaxGroups]>(&s_t[0][0][0]);
+    for (uint32_t e = t; e < ngrp; e += kRefitSeg) {
+        const Box6 y = gload_cg(t2, e);
+        for (int c = 0; c < 3; ++c) {
+            lv[0][c][e] = y.lo[c];
+            lv[0][3 + c][e] = y.hi[c];
+        }
+    }
+    __syncthreads();
 #pragma unroll 1
     for (int k = 1; k < levels2; ++k) {
         const uint32_t half = 1u << (k - 1);
-        const float *prev = t2 + 6 * (size_t)(k - 1) * ngrp;
+        const int a = (k - 1) & 1, o = k & 1;
         for (uint32_t e = t; e < ngrp; e += kRefitSeg) {
-            Box6 y = gload_cg(prev, e);
-            if (e + half < ngrp) y = box_join(y, gload_cg(prev, e + half));
+            Box6 y{{lv[a][0][e], lv[a][1][e], lv[a][2][e]}, {lv[a][3][e], lv[a][4][e], lv[a][5][e]}};
+            if (e + half < ngrp) {
+                const uint32_t f = e + half;
+                y = box_join(y, Box6{{lv[a][0][f], lv[a][1][f], lv[a][2][f]}, {lv[a][3][f], lv[a][4][f], lv[a][5][f]}});
+            }
+            for (int c = 0; c < 3; ++c) {
+                lv[o][c][e] = y.lo[c];
+                lv[o][3 + c][e] = y.hi[c];
+            }
             gstore(t2 + 6 * (size_t)k * ngrp, e, y);
         }
-        __threadfence();
         __syncthreads();
     }
 }
