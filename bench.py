@@ -666,7 +666,7 @@ def run_gb300(args):
     e1.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.steps
     h2d = (3 + 3 + 1) * 4 * nrays
-    d2h = 16 * nrays + 16 * nbounce + 4
+    d2h = 16 * nrays + 16 * nrays + 4   # primary hits, all bounce slots, the bounce count
     e2e_value = rays_per_step * world / (e2e_ms * 1e-3) / 1e6
     # the zero-copy frame gives the same hits as the device-resident one
     torch.cuda.synchronize()
@@ -733,8 +733,8 @@ def run_gb300(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms, "hits_equal_device_run": e2e_same,
                 "how": "one rta_host_frames_run per step on pinned host buffers: rays copied in, frame, "
-                       "primary + bounce hits and bounce count copied out; copies on their own streams "
-                       "overlap the neighbouring steps' traversal"},
+                       "primary hits, all bounce-hit slots and the bounce count copied out; copies on "
+                       "their own streams overlap the neighbouring steps' traversal"},
         # per timed frame: the fused trace (primary + bounce rays) and the
         # bounce gather (the L2 flush between frames is a torch fill)
         "gpu_launches": 2 * args.steps,

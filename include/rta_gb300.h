@@ -205,8 +205,8 @@ int rta_frame_trace_ms(rta_frame_ctx *ctx, float *ms);
  * pinned (cudaHostAlloc / cudaHostRegister).  The rays must be in host memory
  * when the call is made; the outputs are complete once `stream` passes the
  * point where the call left it (the call makes `stream` wait for them).
- * h_bounce_hits needs room for nrays records; *h_bounce_count receives the
- * number written.  Two frames may be in flight; a third waits on the GPU for
+ * h_bounce_hits needs room for nrays records: all nrays are written, the
+ * first *h_bounce_count of them are the frame's bounce hits.  Two frames may be in flight; a third waits on the GPU for
  * its buffers, not on the host. */
 typedef struct rta_host_frames rta_host_frames;
 int rta_host_frames_create(rta_host_frames **out, uint32_t max_rays);

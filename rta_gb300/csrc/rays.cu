@@ -653,16 +653,6 @@ extern "C" int rta_shade_lambert(const void *hits, const void *tris, uint32_t n_
 
 namespace rta {
 
-// the `count` bounce hits of a frame into host memory (device-addressable
-// pinned memory, written over the host link)
-__global__ void k_copy_bounce_hits(const HitRec *__restrict__ src, const uint32_t *__restrict__ count,
-                                   uint32_t cap, float4 *__restrict__ dst)
-{
-    const uint32_t n = min(*count, cap);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        dst[i] = reinterpret_cast<const float4 *>(src)[i];
-}
-
 } // namespace rta
 
 struct rta_host_frames {
@@ -767,9 +757,11 @@ int rta_host_frames_run(rta_host_frames *p, const rta_lbvh *bvh, const float *h_
     RTA_CUDA_TRY(cudaStreamWaitEvent(p->d2h, p->comp_done[k], 0));
     RTA_CUDA_TRY(cudaMemcpyAsync(h_hits, p->hits[k], (size_t)nrays * sizeof(HitRec), cudaMemcpyDeviceToHost, p->d2h));
     RTA_CUDA_TRY(cudaMemcpyAsync(h_bounce_count, &f->fs->count, 4, cudaMemcpyDeviceToHost, p->d2h));
-    const uint32_t blocks = (nrays + 255) / 256 < 1024 ? (nrays + 255) / 256 : 1024;
-    k_copy_bounce_hits<<<blocks, 256, 0, p->d2h>>>(f->hits, &f->fs->count, nrays, (float4 *)h_bounce_hits);
-    if ((rc = check_launch("k_copy_bounce_hits"))) return rc;
+    // all nrays bounce slots (the count is known only on the device): a copy
+    // engine moves them beside the next frame's traversal, where a copy
+    // kernel of exactly `count` records would wait for that frame's blocks
+    RTA_CUDA_TRY(cudaMemcpyAsync(h_bounce_hits, f->hits, (size_t)nrays * sizeof(HitRec), cudaMemcpyDeviceToHost,
+                                 p->d2h));
     RTA_CUDA_TRY(cudaEventRecord(p->out_done[k], p->d2h));
     p->used[k] = true;
     // the caller's stream sees this frame's results once it passes here
