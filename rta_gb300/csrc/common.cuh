@@ -85,6 +85,10 @@ __host__ __device__ __forceinline__ uint32_t make_leaf(uint32_t first, uint32_t 
 __host__ __device__ __forceinline__ float ref_min(float a, float b) { return (a < b) ? a : b; }
 __host__ __device__ __forceinline__ float ref_max(float a, float b) { return (a > b) ? a : b; }
 
+// rays per tile of the bounce compaction kernels (rays.cu); the fused frame
+// counts each tile's bounce rays for the gather
+constexpr int kBounceTileLog2 = 10;
+
 // Bounded spin: every wait on another block gives up after this many polls
 // and raises RTA_DEV_SPIN_TIMEOUT instead of hanging the GPU.
 constexpr uint32_t kSpinLimit = 1u << 22;

@@ -19,7 +19,7 @@ int trace_impl(const rta_lbvh *bvh, const float *orig, const float *dir, const f
                uint32_t *queue, cudaStream_t s);
 int trace_frame_fused(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt, uint32_t nrays,
                       void *hits, uint32_t seed, float eps, float *b_orig, float *b_dir, void *b_hits,
-                      uint32_t *b_flag, uint32_t *queue, cudaStream_t s);
+                      uint32_t *b_flag, uint32_t *b_tile, uint32_t *queue, cudaStream_t s);
 
 __global__ void k_shirley(float *__restrict__ dirs, float *__restrict__ orgs, float *__restrict__ maxts,
                           float height, float aspect, int w, int h, V3 vd, V3 pos, V3 up, float maxt)
@@ -66,6 +66,7 @@ __global__ void k_reset(HitRec *__restrict__ hits, uint32_t n, const uint32_t *_
 constexpr int kBounceThreads = 256;
 constexpr int kBounceItems = 4;
 constexpr int kBounceTile = kBounceThreads * kBounceItems;
+static_assert(kBounceTile == 1 << kBounceTileLog2, "bounce tile");
 
 struct FrameState {
     uint32_t tile_ctr;
@@ -163,23 +164,29 @@ using namespace rta;
 
 // The fused frame's bounce rays and hits, gathered from the per-primary-ray
 // slots into the frame's buffers in primary-ray order (bounce ray k = the k-th
-// flagged ray), with the same single-pass ordered scan as k_bounce.
+// flagged ray).  The trace kernel counted each tile's flagged rays
+// (tile_cnt), so a tile's first output position is the sum of the counts
+// before it: no look-back between tiles.
 __global__ void __launch_bounds__(kBounceThreads)
 k_bounce_gather(const uint32_t *__restrict__ flag, const float *__restrict__ s_orig,
                 const float *__restrict__ s_dir, const HitRec *__restrict__ s_hits, uint32_t nrays,
                 float *__restrict__ oo, float *__restrict__ od, float *__restrict__ om, uint32_t *__restrict__ osrc,
-                HitRec *__restrict__ ohits, uint32_t *__restrict__ tstat, FrameState *__restrict__ fs)
+                HitRec *__restrict__ ohits, const uint32_t *__restrict__ tile_cnt, FrameState *__restrict__ fs)
 {
     constexpr int kWarps = kBounceThreads / 32;
     constexpr int kChunks = kBounceItems * kWarps;
-    __shared__ uint32_t s_tile, s_cnt[kChunks], s_base;
+    __shared__ uint32_t s_cnt[kChunks], s_part[kWarps], s_base;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    if (tid == 0) s_tile = atomicAdd(&fs->tile_ctr, 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
+    const uint32_t tile = blockIdx.x;
     const uint32_t ntiles = (nrays + kBounceTile - 1) / kBounceTile;
     const uint32_t first = tile * kBounceTile + tid;
     const uint32_t lt_mask = (1u << lane) - 1u;
+    // the tiles before this one
+    uint32_t before = 0;
+    for (uint32_t q = tid; q < tile; q += kBounceThreads) before += tile_cnt[q];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) before += __shfl_xor_sync(0xffffffffu, before, off);
+    if (lane == 0) s_part[w] = before;
     bool hit[kBounceItems];
     uint32_t bal[kBounceItems];
 #pragma unroll
@@ -201,16 +208,8 @@ k_bounce_gather(const uint32_t *__restrict__ flag, const float *__restrict__ s_o
         if (lane < kChunks) s_cnt[lane] = x - c;
         const uint32_t run = __shfl_sync(0xffffffffu, x, 31);
         if (lane == 0) {
-            uint32_t *my = tstat + tile;
             uint32_t excl = 0;
-            if (tile == 0) {
-                st_volatile(my, kStatPrefix | run);
-            } else {
-                st_volatile(my, kStatAggregate | run);
-                excl = lookback(tstat, 1, tile, &fs->status);
-                __threadfence();
-                st_volatile(my, kStatPrefix | ((excl + run) & kStatValue));
-            }
+            for (int q = 0; q < kWarps; ++q) excl += s_part[q];
             s_base = excl;
             if (tile == ntiles - 1) fs->count = excl + run;
         }
@@ -350,24 +349,25 @@ int rta_frame_run(rta_frame_ctx *c, const rta_lbvh *bvh, const float *orig, cons
         return RTA_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t mode_nostats = mode & ~RTA_TRACE_STATS;
-    if (c->timing) RTA_CUDA_TRY(cudaEventRecord(c->ev_begin, s));
     if (mode_nostats == RTA_TRACE_CIS) {
         // one launch traces every primary ray and, right after it, its bounce
         // ray; a gather then lays the bounce rays and hits out in primary order
+        const uint32_t tiles = (nrays + kBounceTile - 1) / kBounceTile;
+        RTA_CUDA_TRY(cudaMemsetAsync(c->tstat, 0, (size_t)tiles * 4, s));   // per-tile bounce counts
+        RTA_CUDA_TRY(cudaMemsetAsync(&c->fs->queue, 0, 4, s));
+        if (c->timing) RTA_CUDA_TRY(cudaEventRecord(c->ev_begin, s));
         int rc = trace_frame_fused(bvh, orig, dir, maxt, nrays, hits, seed, eps, c->s_orig, c->s_dir, c->s_hits,
-                                   c->s_flag, &c->fs->queue, s);
+                                   c->s_flag, c->tstat, &c->fs->queue, s);
         if (rc) return rc;
         if (c->timing) {
             RTA_CUDA_TRY(cudaEventRecord(c->ev_end, s));
             c->timed = true;
         }
-        const uint32_t tiles = (nrays + kBounceTile - 1) / kBounceTile;
-        RTA_CUDA_TRY(cudaMemsetAsync(c->tstat, 0, (size_t)tiles * 4, s));
-        RTA_CUDA_TRY(cudaMemsetAsync(&c->fs->tile_ctr, 0, 4, s));
         k_bounce_gather<<<tiles, kBounceThreads, 0, s>>>(c->s_flag, c->s_orig, c->s_dir, c->s_hits, nrays, c->orig,
                                                          c->dir, c->maxt, c->src, c->hits, c->tstat, c->fs);
         return check_launch("k_bounce_gather");
     }
+    if (c->timing) RTA_CUDA_TRY(cudaEventRecord(c->ev_begin, s));
     const uint32_t rb = (nrays + 255) / 256 < 4096 ? (nrays + 255) / 256 : 4096;
     k_reset<<<rb, 256, 0, s>>>((HitRec *)hits, nrays, nullptr);
     int rc = check_launch("k_reset");

@@ -39,6 +39,7 @@ struct TraceArgs {
     float *b_orig, *b_dir;
     HitRec *b_hits;
     uint32_t *b_flag;
+    uint32_t *b_tile;   // bounce rays per 2^kBounceTileLog2 primary rays (zero at launch)
 };
 
 // three-input min / max (sm_100 family); NaN inputs are ignored as by fminf / fmaxf
@@ -705,6 +706,7 @@ __global__ void __launch_bounds__(kTraceThreads, (!DIS && !AILA) ? RTA_TRACE_MIN
                 }
                 const bool bounce = !second && best.t != FLT_MAX && best.ref < A.n_tris;
                 if (!second) A.b_flag[r] = bounce ? 1u : 0u;
+                if (bounce) atomicAdd(A.b_tile + (r >> kBounceTileLog2), 1u);
                 pending = bounce;
                 active = false;
             } else {
@@ -1271,7 +1273,7 @@ static int launch_fused(const TraceArgs &a, cudaStream_t s)
 
 int trace_frame_fused(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt, uint32_t nrays,
                       void *hits, uint32_t seed, float eps, float *b_orig, float *b_dir, void *b_hits,
-                      uint32_t *b_flag, uint32_t *queue, cudaStream_t s)
+                      uint32_t *b_flag, uint32_t *b_tile, uint32_t *queue, cudaStream_t s)
 {
     TraceArgs a;
     a.nodes = (const NodeRec *)bvh->nodes;
@@ -1293,7 +1295,7 @@ int trace_frame_fused(const rta_lbvh *bvh, const float *orig, const float *dir, 
     a.b_dir = b_dir;
     a.b_hits = (HitRec *)b_hits;
     a.b_flag = b_flag;
-    RTA_CUDA_TRY(cudaMemsetAsync(queue, 0, 4, s));
+    a.b_tile = b_tile;   // the caller zeroes *queue and b_tile
     return bvh->morton_bits == 63 ? launch_fused<80>(a, s) : launch_fused<40>(a, s);
 }
 
