@@ -148,10 +148,9 @@ k_batch_morton(const float *__restrict__ cent, uint32_t n, const uint32_t *__res
 
 // every inner node of every mesh; Morton-ordered triangles; ids made local
 __global__ void __launch_bounds__(256)
-k_batch_karras(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ codes, uint32_t *__restrict__ ids,
-               uint32_t n, const MeshRec *__restrict__ meshes, NodeRec *__restrict__ nodes,
-               uint32_t *__restrict__ parents, uint32_t *__restrict__ counters,
-               const float *__restrict__ tris_in, TriRec *__restrict__ tris)
+k_batch_karras(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ codes, uint32_t n,
+               const MeshRec *__restrict__ meshes, NodeRec *__restrict__ nodes, uint32_t *__restrict__ parents,
+               uint32_t *__restrict__ counters)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -160,10 +159,7 @@ k_batch_karras(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ c
     if (li + 1 < mr.n_tris)
         karras_node(codes + mr.tri_off, mr.n_tris, li, nodes + mr.node_off, parents + mr.parent_off,
                     counters + mr.node_off);
-    const uint32_t id = ids[i];
-    const uint32_t lid = id - mr.tri_off;
-    tris[i] = make_tri(tris_in + (size_t)id * kTriFloats, lid);
-    ids[i] = lid;
+    // the Morton-ordered triangles and mesh-local ids are the refit's (k_refit_seg)
 }
 
 // reset_intersections (librta/cuda-kernels.cu:24-44): t, beta, gamma; ref kept
@@ -296,13 +292,12 @@ static int batch_build_impl(rta_batch *b, const void *tris, cudaStream_t s)
     if (rc) return rc;
     b->keys_sorted = ks;
     b->index = vs;
-    k_batch_karras<<<eb, 256, 0, s>>>(ks, b->codes, vs, n, b->meshes_d, b->nodes, b->parents, b->counters, tin,
-                                      b->tris);
+    k_batch_karras<<<eb, 256, 0, s>>>(ks, b->codes, n, b->meshes_d, b->nodes, b->parents, b->counters);
     if ((rc = check_launch("k_batch_karras"))) return rc;
     const uint32_t inner = n - b->meshes;
-    rc = refit_launch<uint32_t, true>(b->codes, n, b->meshes_d, ks, b->nodes, b->parents, b->tris, b->roots, b->rbox,
-                                      b->counters, inner ? inner : 1u, &hdr->n_cross, &hdr->refit_ticket, b->status,
-                                      batch_sms(), s);
+    rc = refit_launch<uint32_t, true>(b->codes, n, b->meshes_d, ks, tin, vs, b->nodes, b->parents, b->tris, b->roots,
+                                      b->rbox, b->counters, inner ? inner : 1u, &hdr->n_cross, &hdr->refit_ticket,
+                                      b->status, batch_sms(), s);
     if (rc) return rc;
     b->built = true;
     return RTA_OK;

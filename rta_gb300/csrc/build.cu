@@ -191,16 +191,16 @@ template <typename Key>
 __global__ void __launch_bounds__(256)
 k_karras(const Key *__restrict__ codes, const uint32_t *__restrict__ ids, uint32_t n,
          NodeRec *__restrict__ nodes, uint32_t *__restrict__ parents, uint32_t *__restrict__ counters,
-         const float *__restrict__ tris_in, TriRec *__restrict__ tris, float *__restrict__ tris_out)
+         const float *__restrict__ tris_in, float *__restrict__ tris_out)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (i + 1 < n) karras_node(codes, n, i, nodes, parents, counters);
-    // invert_triangle_permutation_cuda (:557-578): gather into Morton order
-    const uint32_t id = __ldg(ids + i);
-    const float *src = tris_in + (size_t)id * kTriFloats;
-    tris[i] = make_tri(src, id);
+    // invert_triangle_permutation_cuda (:557-578): the 104-byte records in
+    // Morton order, when asked for (the 48-byte TriRecs are k_refit_seg's)
     if (tris_out) {
+        const uint32_t id = __ldg(ids + i);
+        const float *src = tris_in + (size_t)id * kTriFloats;
         const float2 *s2 = reinterpret_cast<const float2 *>(src);
         float2 *d2 = reinterpret_cast<float2 *>(tris_out + (size_t)i * kTriFloats);
 #pragma unroll
@@ -458,20 +458,20 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
     if (rc) return rc;
     if (bits == 63)
         k_karras<uint64_t><<<eb, 256, 0, s>>>((const uint64_t *)c->codes, c->index, n, c->nodes,
-                                              c->parents, c->counters, tin, c->tris,
+                                              c->parents, c->counters, tin,
                                               (float *)tris_out);
     else
         k_karras<uint32_t><<<eb, 256, 0, s>>>((const uint32_t *)c->codes, c->index, n, c->nodes,
-                                              c->parents, c->counters, tin, c->tris,
+                                              c->parents, c->counters, tin,
                                               (float *)tris_out);
     if ((rc = check_launch("k_karras"))) return rc;
     const uint32_t cap = n > 1 ? n - 1 : 1;
-    rc = bits == 63 ? refit_launch<uint64_t, false>((const uint64_t *)c->codes, n, nullptr, nullptr, c->nodes,
-                                                    c->parents, c->tris, c->root, c->rbox, c->counters, cap,
-                                                    &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s)
-                    : refit_launch<uint32_t, false>((const uint32_t *)c->codes, n, nullptr, nullptr, c->nodes,
-                                                    c->parents, c->tris, c->root, c->rbox, c->counters, cap,
-                                                    &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s);
+    rc = bits == 63 ? refit_launch<uint64_t, false>((const uint64_t *)c->codes, n, nullptr, nullptr, tin, c->index,
+                                                    c->nodes, c->parents, c->tris, c->root, c->rbox, c->counters,
+                                                    cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s)
+                    : refit_launch<uint32_t, false>((const uint32_t *)c->codes, n, nullptr, nullptr, tin, c->index,
+                                                    c->nodes, c->parents, c->tris, c->root, c->rbox, c->counters,
+                                                    cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s);
     if (rc) return rc;
     c->n = n;
     c->last_bits = bits;

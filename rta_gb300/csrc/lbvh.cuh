@@ -621,7 +621,8 @@ namespace {
 template <typename Key, bool BATCH>
 __global__ void __launch_bounds__(kRefitSeg)
 k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__restrict__ meshes,
-            const uint64_t *__restrict__ keys, NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
+            const uint64_t *__restrict__ keys, const float *__restrict__ tris_in, uint32_t *__restrict__ ids,
+            NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
             TriRec *__restrict__ tris, RootRec *__restrict__ roots, float *__restrict__ pre,
             float *__restrict__ suf, float *__restrict__ seg, uint32_t *__restrict__ cross,
             uint32_t *__restrict__ n_cross, uint32_t *__restrict__ flags)
@@ -638,9 +639,17 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
     if (j < n_all) {
         sp = mesh_of<BATCH>(j, n_all, meshes, keys);
         jl = j - sp.tri_off;
-        b = leaf_box(tris[j]);
         if (sp.n > 1u) leaf_pl = parents[sp.parent_off + sp.n - 1u + jl];
         if (jl + 1u < sp.n) q3 = nodes[sp.node_off + jl].q3;
+        // invert_triangle_permutation_cuda (lbvh-kernels.cu:557-578): the
+        // triangle of sorted position j, in Morton order, with its id local
+        // to its mesh (collapse counts land in .w after the table build's
+        // barrier, or in a later kernel)
+        const uint32_t id = ids[j], lid = id - sp.tri_off;
+        const TriRec tr = make_tri(tris_in + (size_t)id * kTriFloats, lid);
+        tris[j] = tr;
+        if (BATCH) ids[j] = lid;
+        b = leaf_box(tr);
     }
     T.build(b);
     bool crosses = false;
@@ -833,18 +842,21 @@ inline RefitLayout refit_layout(uint32_t n)
     return L;
 }
 
-// The refit of n_all leaves after the Karras kernel: tables in rbox
+// The refit of n_all leaves after the Karras kernel; it also writes the
+// Morton-ordered triangles (ids[j] = input index of sorted position j;
+// rewritten local to the mesh in a batch).  Tables in rbox
 // (refit_layout(n_all).total boxes), the crossing list in cross (one word per
 // inner node: cross_cap), *n_cross and *ticket zero on entry.
 template <typename Key, bool BATCH>
-int refit_launch(const Key *codes, uint32_t n_all, const MeshRec *meshes, const uint64_t *keys, NodeRec *nodes,
-                 const uint32_t *parents, TriRec *tris, RootRec *roots, float *rbox, uint32_t *cross,
-                 uint32_t cross_cap, uint32_t *n_cross, uint32_t *ticket, uint32_t *flags, int sms, cudaStream_t s)
+int refit_launch(const Key *codes, uint32_t n_all, const MeshRec *meshes, const uint64_t *keys,
+                 const float *tris_in, uint32_t *ids, NodeRec *nodes, const uint32_t *parents, TriRec *tris,
+                 RootRec *roots, float *rbox, uint32_t *cross, uint32_t cross_cap, uint32_t *n_cross,
+                 uint32_t *ticket, uint32_t *flags, int sms, cudaStream_t s)
 {
     const RefitLayout L = refit_layout(n_all);
     float *pre = rbox + 6 * L.pre, *suf = rbox + 6 * L.suf, *t1 = rbox + 6 * L.t1, *t2 = rbox + 6 * L.t2;
-    k_refit_seg<Key, BATCH><<<L.nseg, kRefitSeg, 0, s>>>(codes, n_all, meshes, keys, nodes, parents, tris, roots,
-                                                         pre, suf, t1, cross, n_cross, flags);
+    k_refit_seg<Key, BATCH><<<L.nseg, kRefitSeg, 0, s>>>(codes, n_all, meshes, keys, tris_in, ids, nodes, parents,
+                                                         tris, roots, pre, suf, t1, cross, n_cross, flags);
     int rc = check_launch("k_refit_seg");
     if (rc) return rc;
     k_refit_top<<<L.ngrp, kRefitSeg, 0, s>>>(t1, L.nseg, t2, L.ngrp, L.levels2, ticket);
