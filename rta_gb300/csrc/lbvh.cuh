@@ -459,11 +459,16 @@ __device__ __forceinline__ void write_slot(NodeRec *nd, uint32_t side, const flo
     }
 }
 
-constexpr uint32_t kRefitSeg = 256;   // leaves per segment = threads per block
-constexpr int kRefitLevels = 8;       // sparse table levels 0..7 (windows of 1..128)
-// groups of 256 segments whose table k_refit_top builds in shared memory (2^25 leaves)
-constexpr uint32_t kMaxGroups = (kMaxTriangles + kRefitSeg * kRefitSeg - 1) / (kRefitSeg * kRefitSeg);
-static_assert(2 * 6 * kMaxGroups <= kRefitLevels * 6 * kRefitSeg, "group table fits the segment table space");
+// 256-leaf segments (48 KB tables, 4 blocks per SM); 128 measured slower
+// (more nodes cross segments: 1M build 0.270 against 0.261 ms)
+#ifndef RTA_REFIT_SEG_LOG2
+#define RTA_REFIT_SEG_LOG2 8
+#endif
+constexpr uint32_t kRefitSeg = 1u << RTA_REFIT_SEG_LOG2;   // leaves per segment = threads per block
+constexpr int kRefitLevels = RTA_REFIT_SEG_LOG2;           // sparse table levels (windows of 1 .. kRefitSeg / 2)
+// group unions whose full table k_refit_top builds in shared memory (two
+// levels in the segment table's space); more go level by level through L2
+constexpr uint32_t kMaxGroups = kRefitLevels * kRefitSeg / 2;
 
 struct Box6 {
     float lo[3], hi[3];
