@@ -117,6 +117,25 @@ def test_build_at_refit_segment_and_group_borders(n):
         assert_build_equals(bvh, codes, lb.ids, lb.nodes)
 
 
+@pytest.mark.parametrize("bits", [30, 63])
+def test_build_signed_zero_ties_match_the_oracle(bits):
+    """Box unions of equal values that differ in sign (-0.0 against +0.0):
+    the oracle's sequential climb keeps the left child's value; the range
+    refit keeps the leftmost leaf's, the same bits for every node."""
+    tris = S.terrain(64, 32, seed=9)
+    pos = tris[:, :9]
+    zero = pos == 0.0
+    assert zero.any()
+    flip = np.zeros_like(zero)
+    flip[1::2] = True   # every other triangle's zero coordinates become -0.0
+    pos[zero & flip] = np.float32(-0.0)
+    assert np.signbit(pos[zero]).any() and (~np.signbit(pos[zero])).any()
+    lb = O.lbvh_build(tris, bits)
+    bvh = gpu_build(tris, bits)
+    codes = lb.codes if bits == 63 else lb.codes.astype(np.uint32)
+    assert_build_equals(bvh, codes, lb.ids, lb.nodes)
+
+
 @pytest.mark.parametrize("digit_bits", [10, 11])
 @pytest.mark.parametrize("bits", [30, 63])
 def test_sort_digit_width_gives_the_same_tree(digit_bits, bits):
