@@ -296,9 +296,14 @@ def learned_eval(args, dev):
                 rd = d.view(-1, 3)[idx].contiguous()
                 model.sample(bvh, ro, rd, m[idx].contiguous())
         samples = model.sample_count()
+        torch.cuda.synchronize()
+        sample_s = time.perf_counter() - t0   # scene generation, builds and recording traces
         loss0 = model.gradient(0, min(samples, 1 << 20))[1]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         loss = model.train(epochs=4, batch=1 << 16, lr=2e-3)
-        train_s = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t0    # 4 epochs of the forward/backward and Adam kernels
         bvh = ctor.build(P.cuda_ftl(make(4)))
         if fam == "terrain":
             o, d, m = _frame_rays(lib, bvh, S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), w=3200, h=1800), 4, dev)
@@ -341,7 +346,7 @@ def learned_eval(args, dev):
         work_p, work_l = float(spn.sum()), float(sln.sum())
         out[fam] = {
             "train_samples": samples, "train_loss_before": loss0, "train_loss_after": loss,
-            "train_s": train_s, "eval_rays": nr,
+            "train_s": train_s, "sample_s": sample_s, "train_epochs": 4, "eval_rays": nr,
             "plain": {"nodes_per_ray": float(spn[0]), "tris_per_ray": float(spn[1]), "ms": tp,
                       "mrays_s": nr / (tp * 1e-3) / 1e6},
             "learned": {"nodes_per_ray": float(sln[0]), "tris_per_ray": float(sln[1]), "ms": tl,

@@ -9,7 +9,8 @@
 //   k_mlp_grad  forward and backward of 32-row tiles per warp, every product
 //               on mma.sync bf16 with fp32 accumulation; weight gradients
 //               accumulate in registers across tiles, then per block in shared
-//               memory, then once per block into the global gradient
+//               memory, then once per block into a partial-sum row, which
+//               k_grad_reduce adds up (no atomics on the 1633 gradients)
 //   k_adam      Adam step on the fp32 master weights, republishes the bf16
 //               weights the kernels read
 #include <cmath>
@@ -74,9 +75,11 @@ __device__ __forceinline__ float bf(float x) { return __bfloat162float(__float2b
 // Gradient of the mean binary cross-entropy (logits vs labels, per-sample
 // weights) over rows [first, first+count) of `samples`, scaled by `scale`,
 // added into grad[kParams]; the weighted loss sum is added into *loss.
+// Each block writes its sums to partial[block * (kParams + 1) ...] (the
+// loss last); k_grad_reduce adds the blocks' sums into the gradient.
 __global__ void __launch_bounds__(kGradWarps * 32)
 k_mlp_grad(const MlpWeights *__restrict__ wg, const Sample *__restrict__ samples, uint32_t first,
-           uint32_t count, float scale, float *__restrict__ grad, float *__restrict__ loss)
+           uint32_t count, float scale, float *__restrict__ partial)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     GradSmem &S = *reinterpret_cast<GradSmem *>(smem_raw);
@@ -244,10 +247,24 @@ k_mlp_grad(const MlpWeights *__restrict__ wg, const Sample *__restrict__ samples
             }
     }
     __syncthreads();
-    for (int i = tid; i < kParams; i += blockDim.x)
-        if (S.grad[i] != 0.f) atomicAdd(&grad[i], S.grad[i]);
-    if (tid == 0) atomicAdd(loss, S.loss);
+    float *out = partial + (size_t)blockIdx.x * (kParams + 1);
+    for (int i = tid; i < kParams; i += blockDim.x) out[i] = S.grad[i];
+    if (tid == 0) out[kParams] = S.loss;
 }
+
+// grad[i] += the blocks' partial sums (i = kParams: the loss)
+__global__ void k_grad_reduce(const float *__restrict__ partial, uint32_t blocks, float *__restrict__ grad,
+                              float *__restrict__ loss)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > (uint32_t)kParams) return;
+    float sum = 0.f;
+    for (uint32_t b = 0; b < blocks; ++b) sum += partial[(size_t)b * (kParams + 1) + i];
+    if (i < (uint32_t)kParams) grad[i] += sum;
+    else *loss += sum;
+}
+
+constexpr uint32_t kGradMaxBlocks = 1024;
 
 // ---- Adam + publishing the bf16 weights ---- //
 
@@ -313,6 +330,7 @@ struct rta_order_model {
     Sample *samples = nullptr;
     uint32_t *counters = nullptr;   // [0] samples written, [1] trace queue
     float *params = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *loss = nullptr;
+    float *partial = nullptr;   // per-block gradient sums of k_mlp_grad
     MlpWeights *weights = nullptr;
     int step = 0;
     uint32_t seed = 0;
@@ -346,6 +364,7 @@ int rta_order_create(rta_order_model **out, uint32_t max_samples, uint32_t seed)
     if (e == cudaSuccess) e = cudaMalloc(&c->m, kParams * 4);
     if (e == cudaSuccess) e = cudaMalloc(&c->v, kParams * 4);
     if (e == cudaSuccess) e = cudaMalloc(&c->grad, kParams * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&c->partial, (size_t)kGradMaxBlocks * (kParams + 1) * 4);
     if (e == cudaSuccess) e = cudaMalloc(&c->loss, 4);
     if (e == cudaSuccess) e = cudaMalloc(&c->weights, sizeof(MlpWeights));
     if (e == cudaSuccess) e = cudaMemset(c->m, 0, kParams * 4);
@@ -376,7 +395,7 @@ int rta_order_create(rta_order_model **out, uint32_t max_samples, uint32_t seed)
 int rta_order_destroy(rta_order_model *c)
 {
     if (!c) return RTA_ERR_INVALID;
-    void *ptrs[] = {c->samples, c->counters, c->params, c->m, c->v, c->grad, c->loss, c->weights};
+    void *ptrs[] = {c->samples, c->counters, c->params, c->m, c->v, c->grad, c->loss, c->weights, c->partial};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete c;
@@ -442,6 +461,21 @@ int rta_order_samples(const rta_order_model *c, void **d_samples)
     return RTA_OK;
 }
 
+// c->grad += the gradient of `scale` x the loss sum over samples [first,
+// first+count), c->loss += that loss sum
+static int grad_step(rta_order_model *c, uint32_t first, uint32_t count, float scale, cudaStream_t s)
+{
+    const uint32_t tiles = (count + 31) / 32;
+    uint32_t blocks = (tiles + kGradWarps - 1) / kGradWarps;
+    if (blocks > kGradMaxBlocks) blocks = kGradMaxBlocks;
+    k_mlp_grad<<<blocks, kGradWarps * 32, sizeof(GradSmem), s>>>(c->weights, c->samples, first, count, scale,
+                                                                  c->partial);
+    int rc = check_launch("k_mlp_grad");
+    if (rc) return rc;
+    k_grad_reduce<<<(kParams + 1 + 255) / 256, 256, 0, s>>>(c->partial, blocks, c->grad, c->loss);
+    return check_launch("k_grad_reduce");
+}
+
 // Gradient of the mean loss over samples [first, first+count) at the current
 // parameters, without an update (for checks against a reference).
 int rta_order_gradient(rta_order_model *c, uint32_t first, uint32_t count, float *host_grad,
@@ -456,11 +490,8 @@ int rta_order_gradient(rta_order_model *c, uint32_t first, uint32_t count, float
                                           (int)sizeof(GradSmem)));
         attr = true;
     }
-    const uint32_t tiles = (count + 31) / 32;
-    const uint32_t blocks = (tiles + kGradWarps - 1) / kGradWarps < 1024 ? (tiles + kGradWarps - 1) / kGradWarps : 1024;
-    k_mlp_grad<<<blocks, kGradWarps * 32, sizeof(GradSmem)>>>(c->weights, c->samples, first, count,
-                                                               1.0f / (float)count, c->grad, c->loss);
-    RTA_CUDA_TRY(cudaGetLastError());
+    int rc = grad_step(c, first, count, 1.0f / (float)count, nullptr);
+    if (rc) return rc;
     RTA_CUDA_TRY(cudaMemcpy(host_grad, c->grad, kParams * 4, cudaMemcpyDeviceToHost));
     float l = 0.f;
     RTA_CUDA_TRY(cudaMemcpy(&l, c->loss, 4, cudaMemcpyDeviceToHost));
@@ -505,11 +536,7 @@ int rta_order_train(rta_order_model *c, uint32_t epochs, uint32_t batch, float l
         for (uint32_t bi = 0; bi < nbatch; ++bi) {
             const uint32_t first = order[bi] * batch;
             const uint32_t cnt = n - first < batch ? n - first : batch;
-            const uint32_t tiles = (cnt + 31) / 32;
-            uint32_t blocks = (tiles + kGradWarps - 1) / kGradWarps;
-            if (blocks > 1024) blocks = 1024;
-            k_mlp_grad<<<blocks, kGradWarps * 32, sizeof(GradSmem), s>>>(c->weights, c->samples, first, cnt,
-                                                                          1.0f / (float)cnt, c->grad, c->loss);
+            if ((rc = grad_step(c, first, cnt, 1.0f / (float)cnt, s))) return rc;
             ++c->step;
             const float c1 = 1.f - std::pow(b1, (float)c->step), c2 = 1.f - std::pow(b2, (float)c->step);
             k_adam<<<1, 1024, 0, s>>>(c->params, c->m, c->v, c->grad, lr, b1, b2, c1, c2, eps, c->weights);
