@@ -64,6 +64,7 @@ k_bounds(const float *__restrict__ tris, uint32_t n, float *__restrict__ cent,
          float *__restrict__ partial, BuildState *__restrict__ st, uint32_t *__restrict__ flags,
          float grid)
 {
+    pdl_enter();
     // init +-1e11 as calculateVoxelBounds does (lbvh-kernels.cu:519-520)
     float lo[3] = {100000000000.0f, 100000000000.0f, 100000000000.0f};
     float hi[3] = {-100000000000.0f, -100000000000.0f, -100000000000.0f};
@@ -162,6 +163,7 @@ k_morton(const float *__restrict__ cent, uint32_t n, Key *__restrict__ keys,
          const BuildState *__restrict__ st, SortScratchHeader *__restrict__ hdr,
          uint32_t *__restrict__ flags, int passes, int dbits, uint32_t grid_mask)
 {
+    pdl_enter();
     extern __shared__ uint32_t s_hist[];
     const int radix = 1 << dbits;
     const uint32_t dmask = (uint32_t)radix - 1u;
@@ -193,6 +195,7 @@ k_karras(const Key *__restrict__ codes, const uint32_t *__restrict__ ids, uint32
          NodeRec *__restrict__ nodes, uint32_t *__restrict__ parents, uint32_t *__restrict__ counters,
          const float *__restrict__ tris_in, float *__restrict__ tris_out)
 {
+    pdl_enter();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (i + 1 < n) karras_node(codes, n, i, nodes, parents, counters);
@@ -339,15 +342,15 @@ static int sort_keys(rta_lbvh_ctx *c, uint32_t n, int passes, SortScratchHeader 
     switch (c->digit_bits) {
     case 10:
         rc = sort_passes_launch<Key, 10>(k0, k1, c->vals0, c->vals1, n, passes, hdr, tstat, c->status, nullptr,
-                                         0u, s, &ks, &vs);
+                                         0u, s, &ks, &vs, true);
         break;
     case 11:
         rc = sort_passes_launch<Key, 11>(k0, k1, c->vals0, c->vals1, n, passes, hdr, tstat, c->status, nullptr,
-                                         0u, s, &ks, &vs);
+                                         0u, s, &ks, &vs, true);
         break;
     default:
         rc = sort_passes_launch<Key, 8>(k0, k1, c->vals0, c->vals1, n, passes, hdr, tstat, c->status, nullptr,
-                                        0u, s, &ks, &vs);
+                                        0u, s, &ks, &vs, true);
     }
     c->codes = ks;
     c->index = vs;
@@ -445,33 +448,31 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
                                           48 * 1024));
         hist_smem_set = true;
     }
-    if (bits == 63)
-        k_morton<uint64_t><<<mb, 256, hsmem, s>>>(c->cent, n, (uint64_t *)c->keys0, c->state, hdr,
-                                                  c->status, passes, db, gmask);
-    else
-        k_morton<uint32_t><<<mb, 256, hsmem, s>>>(c->cent, n, (uint32_t *)c->keys0, c->state, hdr,
-                                                  c->status, passes, db, gmask);
-    if ((rc = check_launch("k_morton"))) return rc;
+    RTA_CUDA_TRY(bits == 63 ? launch_pdl(true, k_morton<uint64_t>, dim3(mb), dim3(256), hsmem, s,
+                                         (const float *)c->cent, n, (uint64_t *)c->keys0,
+                                         (const BuildState *)c->state, hdr, c->status, passes, db, gmask)
+                            : launch_pdl(true, k_morton<uint32_t>, dim3(mb), dim3(256), hsmem, s,
+                                         (const float *)c->cent, n, (uint32_t *)c->keys0,
+                                         (const BuildState *)c->state, hdr, c->status, passes, db, gmask));
 
     rc = bits == 63 ? sort_keys<uint64_t>(c, n, passes, hdr, tstat, s)
                     : sort_keys<uint32_t>(c, n, passes, hdr, tstat, s);
     if (rc) return rc;
-    if (bits == 63)
-        k_karras<uint64_t><<<eb, 256, 0, s>>>((const uint64_t *)c->codes, c->index, n, c->nodes,
-                                              c->parents, c->counters, tin,
-                                              (float *)tris_out);
-    else
-        k_karras<uint32_t><<<eb, 256, 0, s>>>((const uint32_t *)c->codes, c->index, n, c->nodes,
-                                              c->parents, c->counters, tin,
-                                              (float *)tris_out);
-    if ((rc = check_launch("k_karras"))) return rc;
+    RTA_CUDA_TRY(bits == 63 ? launch_pdl(true, k_karras<uint64_t>, dim3(eb), dim3(256), 0, s,
+                                         (const uint64_t *)c->codes, (const uint32_t *)c->index, n, c->nodes,
+                                         c->parents, c->counters, tin, (float *)tris_out)
+                            : launch_pdl(true, k_karras<uint32_t>, dim3(eb), dim3(256), 0, s,
+                                         (const uint32_t *)c->codes, (const uint32_t *)c->index, n, c->nodes,
+                                         c->parents, c->counters, tin, (float *)tris_out));
     const uint32_t cap = n > 1 ? n - 1 : 1;
     rc = bits == 63 ? refit_launch<uint64_t, false>((const uint64_t *)c->codes, n, nullptr, nullptr, tin, c->index,
                                                     c->nodes, c->parents, c->tris, c->root, c->rbox, c->counters,
-                                                    cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s)
+                                                    cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s,
+                                                    true)
                     : refit_launch<uint32_t, false>((const uint32_t *)c->codes, n, nullptr, nullptr, tin, c->index,
                                                     c->nodes, c->parents, c->tris, c->root, c->rbox, c->counters,
-                                                    cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s);
+                                                    cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s,
+                                                    true);
     if (rc) return rc;
     c->n = n;
     c->last_bits = bits;

@@ -89,6 +89,24 @@ __host__ __device__ __forceinline__ float ref_max(float a, float b) { return (a 
 // counts each tile's bounce rays for the gather
 constexpr int kBounceTileLog2 = 10;
 
+// Programmatic dependent launch along the build's kernel chain: a kernel
+// launched by launch_pdl may start while the previous kernel of its stream
+// drains.  Every chained kernel first waits for the previous kernel's
+// completion and memory (griddepcontrol.wait) before it touches memory, then
+// lets the next kernel launch (griddepcontrol.launch_dependents), which
+// happens once all of its own blocks have started.  For a kernel launched
+// without the attribute both instructions do nothing.
+#ifndef RTA_PDL
+#define RTA_PDL 1
+#endif
+__device__ __forceinline__ void pdl_enter()
+{
+#if RTA_PDL
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
 // Bounded spin: every wait on another block gives up after this many polls
 // and raises RTA_DEV_SPIN_TIMEOUT instead of hanging the GPU.
 constexpr uint32_t kSpinLimit = 1u << 22;
@@ -159,7 +177,25 @@ namespace rta {
 void set_cuda_error(cudaError_t e, const char *where);
 void set_error_message(const char *msg);
 int check_launch(const char *where);
+
+// a kernel launch that may overlap the previous kernel of the stream (above)
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = (RTA_PDL && pdl) ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
+} // namespace rta
 
 #define RTA_CUDA_TRY(call)                                                                   \
     do {                                                                                     \

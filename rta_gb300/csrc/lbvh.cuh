@@ -176,6 +176,7 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
            const uint32_t *__restrict__ hist, uint32_t *__restrict__ tstat, uint32_t *__restrict__ flags,
            uint32_t *__restrict__ code_out, uint32_t code_mask)
 {
+    pdl_enter();
     constexpr int kRadix = 1 << BITS;
     constexpr uint32_t kDigitMask = (uint32_t)kRadix - 1u;
     constexpr int kDpt = kRadix > kSortThreads ? kRadix / kSortThreads : 1;   // digits per thread
@@ -295,7 +296,8 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
 template <typename Key, int BITS>
 int sort_passes_launch(Key *k0, Key *k1, uint32_t *v0, uint32_t *v1, uint32_t n, int passes,
                        SortScratchHeader *hdr, uint32_t *tstat, uint32_t *flags, uint32_t *code_out,
-                       uint32_t code_mask, cudaStream_t s, Key **keys_sorted, uint32_t **vals_sorted)
+                       uint32_t code_mask, cudaStream_t s, Key **keys_sorted, uint32_t **vals_sorted,
+                       bool pdl = false)
 {
     constexpr int kRadix = 1 << BITS;
     static bool smem_set = false;
@@ -310,11 +312,15 @@ int sort_passes_launch(Key *k0, Key *k1, uint32_t *v0, uint32_t *v1, uint32_t n,
     uint32_t *vin = nullptr, *vout = v0;
     for (int p = 0; p < passes; ++p) {
         uint32_t *ts = tstat + (size_t)p * tiles * kRadix;
-        k_onesweep<Key, BITS><<<tiles, kSortThreads, smem, s>>>(
-            kin, vin, kout, vout, n, BITS * p, hdr->tile_ctr + p, hdr->hist + (size_t)p * kRadix, ts, flags,
-            p == passes - 1 ? code_out : nullptr, code_mask);
-        int rc = check_launch("k_onesweep");
-        if (rc) return rc;
+        const cudaError_t e =
+            launch_pdl(pdl, k_onesweep<Key, BITS>, dim3(tiles), dim3(kSortThreads), smem, s, kin,
+                       (const uint32_t *)vin, kout, vout, n, BITS * p, hdr->tile_ctr + p,
+                       (const uint32_t *)(hdr->hist + (size_t)p * kRadix), ts, flags,
+                       p == passes - 1 ? code_out : nullptr, code_mask);
+        if (e != cudaSuccess) {
+            set_cuda_error(e, "k_onesweep");
+            return RTA_ERR_CUDA;
+        }
         std::swap(kin, kout);
         vin = vout;
         vout = (vout == v0) ? v1 : v0;
@@ -632,6 +638,7 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
             float *__restrict__ suf, float *__restrict__ seg, uint32_t *__restrict__ cross,
             uint32_t *__restrict__ n_cross, uint32_t *__restrict__ flags)
 {
+    pdl_enter();
     __shared__ float s_t[kRefitLevels][6][kRefitSeg];
     SegTable T{s_t};
     const uint32_t t = threadIdx.x, base = blockIdx.x * kRefitSeg, j = base + t;
@@ -707,6 +714,7 @@ __global__ void __launch_bounds__(kRefitSeg)
 k_refit_top(float *__restrict__ t1, uint32_t nseg, float *__restrict__ t2, uint32_t ngrp, int levels2,
             uint32_t *__restrict__ ticket)
 {
+    pdl_enter();
     __shared__ float s_t[kRefitLevels][6][kRefitSeg];
     SegTable T{s_t};
     const uint32_t t = threadIdx.x, base = blockIdx.x * kRefitSeg, i = base + t;
@@ -818,6 +826,7 @@ k_refit_ext(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
             const float *__restrict__ t2, uint32_t ngrp, const uint32_t *__restrict__ cross,
             const uint32_t *__restrict__ n_cross, uint32_t cross_cap, uint32_t *__restrict__ flags)
 {
+    pdl_enter();
     const uint32_t count = min(*n_cross, cross_cap);
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x)
         refit_cross<Key, BATCH>(codes, n_all, cross[e], meshes, keys, nodes, parents, tris, roots, pre, suf, t1,
@@ -856,22 +865,26 @@ template <typename Key, bool BATCH>
 int refit_launch(const Key *codes, uint32_t n_all, const MeshRec *meshes, const uint64_t *keys,
                  const float *tris_in, uint32_t *ids, NodeRec *nodes, const uint32_t *parents, TriRec *tris,
                  RootRec *roots, float *rbox, uint32_t *cross, uint32_t cross_cap, uint32_t *n_cross,
-                 uint32_t *ticket, uint32_t *flags, int sms, cudaStream_t s)
+                 uint32_t *ticket, uint32_t *flags, int sms, cudaStream_t s, bool pdl = false)
 {
     const RefitLayout L = refit_layout(n_all);
     float *pre = rbox + 6 * L.pre, *suf = rbox + 6 * L.suf, *t1 = rbox + 6 * L.t1, *t2 = rbox + 6 * L.t2;
-    k_refit_seg<Key, BATCH><<<L.nseg, kRefitSeg, 0, s>>>(codes, n_all, meshes, keys, tris_in, ids, nodes, parents,
-                                                         tris, roots, pre, suf, t1, cross, n_cross, flags);
-    int rc = check_launch("k_refit_seg");
-    if (rc) return rc;
-    k_refit_top<<<L.ngrp, kRefitSeg, 0, s>>>(t1, L.nseg, t2, L.ngrp, L.levels2, ticket);
-    if ((rc = check_launch("k_refit_top"))) return rc;
-    if (n_all > 2u) {
+    cudaError_t e = launch_pdl(pdl, k_refit_seg<Key, BATCH>, dim3(L.nseg), dim3(kRefitSeg), 0, s, codes, n_all,
+                               meshes, keys, tris_in, ids, nodes, parents, tris, roots, pre, suf, t1, cross,
+                               n_cross, flags);
+    if (e == cudaSuccess)
+        e = launch_pdl(pdl, k_refit_top, dim3(L.ngrp), dim3(kRefitSeg), 0, s, t1, L.nseg, t2, L.ngrp, L.levels2,
+                       ticket);
+    if (e == cudaSuccess && n_all > 2u) {
         const uint32_t want = (n_all + 255u) / 256u, cap = (uint32_t)sms * 4u;
-        k_refit_ext<Key, BATCH><<<want < cap ? want : cap, 256, 0, s>>>(codes, n_all, meshes, keys, nodes, parents,
-                                                                        tris, roots, pre, suf, t1, L.nseg, t2,
-                                                                        L.ngrp, cross, n_cross, cross_cap, flags);
-        if ((rc = check_launch("k_refit_ext"))) return rc;
+        e = launch_pdl(pdl, k_refit_ext<Key, BATCH>, dim3(want < cap ? want : cap), dim3(256), 0, s, codes, n_all,
+                       meshes, keys, (NodeRec *)nodes, parents, tris, roots, (const float *)pre,
+                       (const float *)suf, (const float *)t1, L.nseg, (const float *)t2, L.ngrp,
+                       (const uint32_t *)cross, (const uint32_t *)n_cross, cross_cap, flags);
+    }
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "refit");
+        return RTA_ERR_CUDA;
     }
     return RTA_OK;
 }
