@@ -77,6 +77,10 @@ typedef struct rta_lbvh {
     uint32_t n;
     int32_t morton_bits;
     uint32_t *status;        /* device word of RTA_DEV_* flags */
+    void *ready;             /* a cudaEvent_t recorded on the build's stream after the
+                              * last build of this tree (NULL for batch meshes):
+                              * calls that read the tree on streams of their own
+                              * (rta_host_frames_run) wait for it */
 } rta_lbvh;
 
 /* new/delete of lbvh_constructor (lbvh.h:114-145) */
@@ -203,8 +207,12 @@ int rta_frame_trace_ms(rta_frame_ctx *ctx, float *ms);
  * device buffers used in turn, so consecutive calls overlap one frame's
  * copies with the neighbouring frames' traversal.  Host pointers must be
  * pinned (cudaHostAlloc / cudaHostRegister).  The rays must be in host memory
- * when the call is made; the outputs are complete once `stream` passes the
- * point where the call left it (the call makes `stream` wait for them).
+ * when the call is made; the frame's traversal waits for bvh->ready, so a
+ * tree built on `stream` (or any stream) just before the call is complete
+ * before it is read; the outputs are complete once `stream` passes the
+ * point where the call left it (the call makes `stream` wait for them), so
+ * work queued on `stream` afterwards, a rebuild of the tree included, runs
+ * after this frame.
  * h_bounce_hits needs room for nrays records: all nrays are written, the
  * first *h_bounce_count of them are the frame's bounce hits.  Two frames may be in flight; a third waits on the GPU for
  * its buffers, not on the host. */
@@ -225,16 +233,20 @@ int rta_host_frames_run(rta_host_frames *frames, const rta_lbvh *bvh, const floa
  * every GPU loading the library holds until the process exits.
  *   out_orig/out_dir/out_maxt/out_src  room for nrays bounce rays
  *   out_count  device word: the number of bounce rays written
+ *   out_flags  optional device word (nullable): the call's RTA_DEV_* flags;
+ *              RTA_DEV_SPIN_TIMEOUT means a bounded wait of the ordered
+ *              compaction gave up and the count and ray order are not valid
  * nrays above RTA_BOUNCE_NOALLOC_MAX_RAYS returns RTA_ERR_INVALID with a
- * message in rta_last_error().  The first call on a device looks up the
- * scratch's device address; make that first call before any stream capture.
+ * message in rta_last_error().  The first call on a device (and the first
+ * after its context was destroyed and created again) looks up the scratch's
+ * device address; make that first call before any stream capture.
  * Every call shares the scratch: calls that overlap on the GPU (other
  * streams, other host threads) race and must be serialised by the caller. */
 #define RTA_BOUNCE_NOALLOC_MAX_RAYS (1u << 24)
 int rta_diffuse_bounce_noalloc(const rta_lbvh *bvh, const float *orig, const float *dir,
                                const void *hits, uint32_t nrays, uint32_t seed, float eps,
                                float *out_orig, float *out_dir, float *out_maxt, uint32_t *out_src,
-                               uint32_t *out_count, rta_stream_t stream);
+                               uint32_t *out_count, uint32_t *out_flags, rta_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
 /* learned child order (no reference counterpart): a 14-32-32-1 network      */

@@ -513,6 +513,7 @@ int rta_batch_mesh(const rta_batch *b, uint32_t mesh, rta_lbvh *out)
     out->n = mr.n_tris;
     out->morton_bits = 30;
     out->status = b->status;
+    out->ready = nullptr;   // the caller orders the batch build before other streams' use
     return RTA_OK;
 }
 

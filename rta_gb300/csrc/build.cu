@@ -297,6 +297,9 @@ struct rta_lbvh_ctx {
     int last_bits = 30;
     void *codes = nullptr;       // sorted keys (keys0 or keys1)
     uint32_t *index = nullptr;   // sorted ids (vals0 or vals1)
+    // recorded on the build's stream after each build's last kernel: work on
+    // other streams that reads the tree waits for it (rta_lbvh::ready)
+    cudaEvent_t built = nullptr;
 };
 
 static int bounds_blocks(uint32_t n)
@@ -327,8 +330,10 @@ static void free_ctx(rta_lbvh_ctx *c)
     for (void *p : ptrs)
         if (p) cudaFree(p);
     const int db = c->digit_bits;
+    cudaEvent_t built = c->built;
     *c = rta_lbvh_ctx();
     c->digit_bits = db;
+    c->built = built;
 }
 
 template <typename Key>
@@ -374,6 +379,7 @@ int rta_lbvh_destroy(rta_lbvh_ctx *ctx)
 {
     if (!ctx) return RTA_ERR_INVALID;
     free_ctx(ctx);
+    if (ctx->built) cudaEventDestroy(ctx->built);
     delete ctx;
     return RTA_OK;
 }
@@ -474,6 +480,8 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
                                                     cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s,
                                                     true);
     if (rc) return rc;
+    if (!c->built) RTA_CUDA_TRY(cudaEventCreateWithFlags(&c->built, cudaEventDisableTiming));
+    RTA_CUDA_TRY(cudaEventRecord(c->built, s));
     c->n = n;
     c->last_bits = bits;
     return RTA_OK;
@@ -491,6 +499,7 @@ int rta_lbvh_get(const rta_lbvh_ctx *c, rta_lbvh *out)
     out->n = c->n;
     out->morton_bits = c->last_bits;
     out->status = c->status;
+    out->ready = c->built;
     return RTA_OK;
 }
 

@@ -10,6 +10,8 @@
 #include <cstring>
 #include <mutex>
 
+#include <cuda.h>
+
 #include "bounce.cuh"
 
 namespace rta {
@@ -74,6 +76,8 @@ struct FrameState {
     uint32_t queue;
     uint32_t status;
 };
+// the allocation-free bounce keeps a FrameState in the first 4 words of its scratch
+static_assert(sizeof(FrameState) == 16, "FrameState is four 32-bit words");
 
 __global__ void __launch_bounds__(kBounceThreads)
 k_bounce(const TriRec *__restrict__ tris, const float *__restrict__ orig, const float *__restrict__ dir,
@@ -436,10 +440,56 @@ static_assert(RTA_BOUNCE_NOALLOC_MAX_RAYS % kBounceTile == 0, "whole tiles");
 constexpr uint32_t kNoAllocWords = 4u + RTA_BOUNCE_NOALLOC_MAX_RAYS / kBounceTile;
 static __device__ __align__(256) uint32_t g_bounce_scratch[kNoAllocWords];
 
-// host side: the device address of g_bounce_scratch, looked up once per device
+// host side: the device address of g_bounce_scratch, looked up once per
+// device and context.  A context that was destroyed (cudaDeviceReset) and
+// created again reloads the module, possibly at another address, so the
+// cached address is keyed on the context's unique id (cuCtxGetId), which the
+// driver never reuses.  The driver calls are fetched through the runtime, so
+// the library does not link libcuda.
 constexpr int kMaxDevices = 64;
 static std::mutex g_scratch_mu;
 static uint32_t *g_scratch_addr[kMaxDevices];
+static unsigned long long g_scratch_ctx[kMaxDevices];
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+static int current_context_id(int dev, unsigned long long *id)
+{
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *f0 = nullptr, *f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = q0;
+        RTA_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0));
+        RTA_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1));
+        if (q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1) {
+            set_error_message("rta_diffuse_bounce_noalloc: the driver lacks cuCtxGetCurrent / cuCtxGetId");
+            return RTA_ERR_CUDA;
+        }
+        get_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+        get_id = reinterpret_cast<CtxGetIdFn>(f1);
+    }
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS) {
+        set_error_message("rta_diffuse_bounce_noalloc: cuCtxGetCurrent failed");
+        return RTA_ERR_CUDA;
+    }
+    if (!ctx) {
+        // no context bound to this thread yet: make the device's primary
+        // context current (cudaSetDevice initialises it)
+        RTA_CUDA_TRY(cudaSetDevice(dev));
+        if (get_current(&ctx) != CUDA_SUCCESS || !ctx) {
+            set_error_message("rta_diffuse_bounce_noalloc: no CUDA context");
+            return RTA_ERR_CUDA;
+        }
+    }
+    if (get_id(ctx, id) != CUDA_SUCCESS) {
+        set_error_message("rta_diffuse_bounce_noalloc: cuCtxGetId failed");
+        return RTA_ERR_CUDA;
+    }
+    return RTA_OK;
+}
 
 static int bounce_scratch(uint32_t **out)
 {
@@ -447,12 +497,16 @@ static int bounce_scratch(uint32_t **out)
     RTA_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return RTA_ERR_INVALID;
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
+    unsigned long long ctx_id = 0;
+    int rc = current_context_id(dev, &ctx_id);
+    if (rc) return rc;
+    if (!g_scratch_addr[dev] || g_scratch_ctx[dev] != ctx_id) {
         // The symbol's name is a host-side stand-in; only this call gives the
         // address the kernels of the current device may use.
         void *p = nullptr;
         RTA_CUDA_TRY(cudaGetSymbolAddress(&p, g_bounce_scratch));
         g_scratch_addr[dev] = static_cast<uint32_t *>(p);
+        g_scratch_ctx[dev] = ctx_id;
     }
     *out = g_scratch_addr[dev];
     return RTA_OK;
@@ -471,7 +525,8 @@ static void g_bounce_noalloc_limit_error(uint32_t nrays)
 extern "C" int rta_diffuse_bounce_noalloc(const rta_lbvh *bvh, const float *orig, const float *dir,
                                           const void *hits, uint32_t nrays, uint32_t seed, float eps,
                                           float *out_orig, float *out_dir, float *out_maxt,
-                                          uint32_t *out_src, uint32_t *out_count, rta_stream_t stream)
+                                          uint32_t *out_src, uint32_t *out_count, uint32_t *out_flags,
+                                          rta_stream_t stream)
 {
     if (!bvh || !orig || !dir || !hits || !out_orig || !out_dir || !out_maxt || !out_src ||
         !out_count || nrays == 0)
@@ -493,6 +548,9 @@ extern "C" int rta_diffuse_bounce_noalloc(const rta_lbvh *bvh, const float *orig
                                               scratch + 4, fs, bvh->n);
     if ((rc = check_launch("k_bounce (noalloc)"))) return rc;
     RTA_CUDA_TRY(cudaMemcpyAsync(out_count, &fs->count, 4, cudaMemcpyDeviceToDevice, s));
+    // the call's device flags (a look-back wait that gave up leaves the
+    // count and the ray order undefined); the next call clears the scratch
+    if (out_flags) RTA_CUDA_TRY(cudaMemcpyAsync(out_flags, &fs->status, 4, cudaMemcpyDeviceToDevice, s));
     return RTA_OK;
 }
 
@@ -748,8 +806,10 @@ int rta_host_frames_run(rta_host_frames *p, const rta_lbvh *bvh, const float *h_
     RTA_CUDA_TRY(cudaMemcpyAsync(p->dir[k], h_dir, (size_t)nrays * 12, cudaMemcpyHostToDevice, p->h2d));
     RTA_CUDA_TRY(cudaMemcpyAsync(p->maxt[k], h_maxt, (size_t)nrays * 4, cudaMemcpyHostToDevice, p->h2d));
     RTA_CUDA_TRY(cudaEventRecord(p->in_done[k], p->h2d));
-    // the frame
+    // the frame, once its rays are in and the tree's last build (on whatever
+    // stream it was issued) is complete
     RTA_CUDA_TRY(cudaStreamWaitEvent(p->comp, p->in_done[k], 0));
+    if (bvh->ready) RTA_CUDA_TRY(cudaStreamWaitEvent(p->comp, (cudaEvent_t)bvh->ready, 0));
     int rc = rta_frame_run(f, bvh, p->orig[k], p->dir[k], p->maxt[k], nrays, p->hits[k], mode, seed, eps, p->comp);
     if (rc) return rc;
     RTA_CUDA_TRY(cudaEventRecord(p->comp_done[k], p->comp));

@@ -44,7 +44,8 @@ class LbvhView(C.Structure):
     """struct rta_lbvh"""
     _fields_ = [("nodes", C.c_void_p), ("root", C.c_void_p), ("tris", C.c_void_p),
                 ("index", C.c_void_p), ("codes", C.c_void_p), ("parents", C.c_void_p),
-                ("n", C.c_uint32), ("morton_bits", C.c_int32), ("status", C.c_void_p)]
+                ("n", C.c_uint32), ("morton_bits", C.c_int32), ("status", C.c_void_p),
+                ("ready", C.c_void_p)]
 
 
 class FrameView(C.Structure):
@@ -115,7 +116,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_trace_learned.argtypes = [P(LbvhView), vp, vp, vp, vp, u32, vp, vp, vp, vp]
     L.rta_trace_ideal_order.argtypes = [P(LbvhView), vp, vp, vp, u32, vp, vp, vp, vp]
     L.rta_diffuse_bounce_noalloc.argtypes = [P(LbvhView), vp, vp, vp, u32, u32, f32, vp, vp, vp, vp,
-                                             vp, vp]
+                                             vp, vp, vp]
     L.rta_shade_lambert.argtypes = [vp, vp, u32, u32, u32, vp, u32, i32, vp, vp, vp, vp]
     L.rta_batch_create.argtypes = [P(vp)]
     L.rta_batch_destroy.argtypes = [vp]

@@ -1,6 +1,6 @@
 """Generates the golden fixtures in this folder from the reference itself.
 
-Needs the reference sources (default /root/reference, or $RTA_REFERENCE): the
+Needs the reference sources ($RTA_REFERENCE, else a checkout beside this repository): the
 recipe in oracle/refbuild compiles
 
 * the reference CPU plugin bbvh.so (bbvh/) driven through rta's plugin ABI,
@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 
 from rta_gb300 import scenes as S  # noqa: E402
 
-REF = os.environ.get("RTA_REFERENCE", "/root/reference")
+REF = os.environ.get("RTA_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
 OUT = os.path.dirname(os.path.abspath(__file__))
 REFDIR = os.path.join(ROOT, "oracle", "_ref")
 HIT = np.dtype([("t", "<f4"), ("beta", "<f4"), ("gamma", "<f4"), ("ref", "<u4")])

@@ -360,22 +360,120 @@ def test_rebinding_contract():
 # full configuration-2 size                                                    #
 # --------------------------------------------------------------------------- #
 
-def test_full_size_terrain_build_and_frame():
+class _FullTerrain:
+    """The benchmarked configuration: the 1,048,576-triangle terrain (seed
+    0), its 1920x1080 camera frame and one diffuse bounce per hit (seed 0,
+    eps 1e-4), all computed by the oracle once per module."""
+
+    def __init__(self):
+        self.tris = S.terrain(1024, 512, seed=0)
+        self.lb = O.lbvh_build(self.tris, 30)
+        self.srt = O.permute(self.tris, self.lb.ids)
+        cam = S.terrain_camera()
+        self.cam = cam
+        self.o, self.d, self.m = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
+        self.ref, _, _ = O.trace(self.lb.nodes, self.srt, self.o, self.d, self.m, O.CIS, 64)
+        self.bo, self.bd, self.bm, self.bsrc = O.diffuse_bounce(self.srt, self.o, self.d, self.ref, seed=0,
+                                                                eps=1e-4)
+        self.bref, _, _ = O.trace(self.lb.nodes, self.srt, self.bo, self.bd, self.bm, O.CIS, 64)
+
+
+@pytest.fixture(scope="module")
+def full_terrain():
+    return _FullTerrain()
+
+
+def test_full_size_terrain_build_and_frame(full_terrain):
     """1,048,576-triangle terrain and the 1920x1080 frame: the whole tree is
     bit-identical to the oracle's, and so is every primary hit."""
-    tris = S.terrain(1024, 512, seed=0)
-    lb = O.lbvh_build(tris, 30)
-    bvh = gpu_build(tris, 30)
+    ft = full_terrain
+    bvh = gpu_build(ft.tris, 30)
     codes = bvh.codes()
     assert (np.diff(codes.astype(np.int64)) >= 0).all()
     ids = bvh.index_buffer
-    assert np.array_equal(np.sort(ids), np.arange(tris.shape[0], dtype=np.uint32))
-    assert_build_equals(bvh, lb.codes.astype(np.uint32), lb.ids, lb.nodes)
-    cam = S.terrain_camera()
-    o, d, m = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
-    srt = O.permute(tris, lb.ids)
-    ref, _, _ = O.trace(lb.nodes, srt, o, d, m, O.CIS, 64)
-    assert_hits_equal(gpu_trace(bvh, o, d, m, L.TRACE_CIS), ref)
+    assert np.array_equal(np.sort(ids), np.arange(ft.tris.shape[0], dtype=np.uint32))
+    assert_build_equals(bvh, ft.lb.codes.astype(np.uint32), ft.lb.ids, ft.lb.nodes)
+    assert_hits_equal(gpu_trace(bvh, ft.o, ft.d, ft.m, L.TRACE_CIS), ft.ref)
+
+
+def _device(a, dtype=np.float32):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype).reshape(-1).copy()).to("cuda")
+
+
+def test_full_size_fused_frame_matches_oracle(full_terrain):
+    """The benchmarked frame exactly as bench.py times it: rta_frame_run (the
+    fused primary + bounce trace launch and the bounce gather) on the
+    1,048,576-triangle terrain at 1920x1080, seed 0, eps 1e-4.  Every primary
+    hit, the bounce count, every bounce ray (origin, direction, max_t, source
+    pixel) and every bounce hit equal the oracle's, bit for bit."""
+    import ctypes as C
+    ft = full_terrain
+    bvh = gpu_build(ft.tris, 30)
+    n = ft.m.shape[0]
+    o, d, m = _device(ft.o), _device(ft.d), _device(ft.m)
+    hits = torch.empty(4 * n, dtype=torch.float32, device="cuda")
+    lib = L.load()
+    fh = C.c_void_p()
+    L.check(lib.rta_frame_create(C.byref(fh), n), "rta_frame_create")
+    try:
+        f = L.FrameView()
+        L.check(lib.rta_frame_get(fh, C.byref(f)), "rta_frame_get")
+        for _ in range(2):   # the second run reuses the frame's buffers and counters
+            hits.fill_(0)
+            L.check(lib.rta_frame_run(fh, C.byref(bvh.view), P._ptr(o), P._ptr(d), P._ptr(m), n, P._ptr(hits),
+                                      L.TRACE_CIS, 0, np.float32(1e-4), P._stream()), "rta_frame_run")
+            flags = C.c_uint32(0)
+            L.check(lib.rta_frame_status(fh, P._stream(), C.byref(flags)), "rta_frame_status")
+            assert flags.value == 0
+            assert_hits_equal(hits.cpu().numpy().view(O.HIT_DTYPE), ft.ref)
+            cnt = int(P.device_view(f.count, 1, "<u4").cpu().numpy().view(np.uint32)[0])
+            assert cnt == ft.bm.shape[0] > 700000
+            np.testing.assert_array_equal(P.device_view(f.src, cnt, "<u4").cpu().numpy().view(np.uint32), ft.bsrc)
+            np.testing.assert_array_equal(P.device_view(f.orig, 3 * cnt).cpu().numpy().view(np.uint32),
+                                          ft.bo.reshape(-1).view(np.uint32))
+            np.testing.assert_array_equal(P.device_view(f.dir, 3 * cnt).cpu().numpy().view(np.uint32),
+                                          ft.bd.reshape(-1).view(np.uint32))
+            np.testing.assert_array_equal(P.device_view(f.maxt, cnt).cpu().numpy().view(np.uint32),
+                                          ft.bm.view(np.uint32))
+            assert_hits_equal(P.device_view(f.hits, 4 * cnt).cpu().numpy().view(O.HIT_DTYPE), ft.bref)
+    finally:
+        lib.rta_frame_destroy(fh)
+
+
+def test_full_size_host_frames_match_oracle(full_terrain):
+    """The e2e path of the bench, rta_host_frames_run on pinned host buffers,
+    at full size.  The tree is rebuilt on a side stream behind a delay and
+    the frames are queued on that stream with no host synchronisation: the
+    frames' own streams must wait for the rebuild (rta_lbvh::ready), so the
+    hits are the new tree's.  Three frames in a row use both buffer sets."""
+    ft = full_terrain
+    n = ft.m.shape[0]
+    ctor = P.lbvh_constructor(morton_bits=30)
+    # another tree of the same size first, so the rebuild reuses the buffers
+    # (a reallocation would synchronise the device and hide the ordering)
+    ctor.build(P.cuda_ftl(S.terrain(1024, 512, seed=7)))
+    torch.cuda.synchronize()
+    ho = torch.from_numpy(np.ascontiguousarray(ft.o, np.float32).reshape(-1)).pin_memory()
+    hd = torch.from_numpy(np.ascontiguousarray(ft.d, np.float32).reshape(-1)).pin_memory()
+    hm = torch.from_numpy(np.ascontiguousarray(ft.m, np.float32).reshape(-1)).pin_memory()
+    outs = [(torch.zeros(4 * n, dtype=torch.float32).pin_memory(),
+             torch.zeros(4 * n, dtype=torch.float32).pin_memory(),
+             torch.zeros(1, dtype=torch.int32).pin_memory()) for _ in range(3)]
+    tri_dev = P.cuda_ftl(ft.tris)
+    hf = P.host_frames(n)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())   # the triangle upload
+    with torch.cuda.stream(side):
+        torch.cuda._sleep(200_000_000)   # about 0.1 s of GPU time before the rebuild starts
+        bvh = ctor.build(tri_dev)
+        for h_hits, h_bhits, h_cnt in outs:
+            hf.run(bvh, ho, hd, hm, h_hits, h_bhits, h_cnt, L.TRACE_CIS, 0, 1e-4, n)
+    side.synchronize()
+    nb = ft.bm.shape[0]
+    for h_hits, h_bhits, h_cnt in outs:
+        assert int(h_cnt.item()) == nb
+        assert_hits_equal(h_hits.numpy().view(O.HIT_DTYPE), ft.ref)
+        assert_hits_equal(h_bhits.numpy().view(O.HIT_DTYPE)[:nb], ft.bref)
 
 
 def test_full_size_incoherent_clusters_build_and_trace():

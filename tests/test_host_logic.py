@@ -7,7 +7,8 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REFERENCE = os.environ.get("RTA_REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("RTA_REFERENCE") or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "reference")
 
 
 def _rank_main(rank, world, port, q):

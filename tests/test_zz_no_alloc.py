@@ -17,15 +17,37 @@ import pytest
 from rta_gb300 import lib as L
 
 
+def _no_gpu():
+    try:
+        import torch
+        return not torch.cuda.is_available()
+    except ImportError:
+        return True
+
+
 def test_rejects_more_rays_than_the_scratch_holds():
     lib = L.load()
     view = L.LbvhView()
     view.tris, view.n = 16, 1
     fake = C.c_void_p(256)
     rc = lib.rta_diffuse_bounce_noalloc(C.byref(view), fake, fake, fake, L.BOUNCE_NOALLOC_MAX_RAYS + 1, 0,
-                                        1e-4, fake, fake, fake, fake, fake, None)
+                                        1e-4, fake, fake, fake, fake, fake, None, None)
     assert rc == L.ERR_INVALID
     assert b"exceed" in lib.rta_last_error()
+
+
+@pytest.mark.skipif(not _no_gpu(), reason="fake pointers: only where no GPU can run the kernel")
+def test_accepts_exactly_the_scratch_limit():
+    """RTA_BOUNCE_NOALLOC_MAX_RAYS itself passes the size check: without a
+    GPU the call then fails at the device lookup, not on the argument."""
+    lib = L.load()
+    view = L.LbvhView()
+    view.tris, view.n = 16, 1
+    fake = C.c_void_p(256)
+    rc = lib.rta_diffuse_bounce_noalloc(C.byref(view), fake, fake, fake, L.BOUNCE_NOALLOC_MAX_RAYS, 0,
+                                        1e-4, fake, fake, fake, fake, fake, None, None)
+    assert rc == L.ERR_CUDA
+    assert b"exceed" not in lib.rta_last_error()
 
 
 @pytest.mark.gpu
@@ -77,21 +99,54 @@ def test_noalloc_bounce_matches_allocating_entry_point_twice():
         om = torch.empty(n, dtype=torch.float32, device=dev)
         src = torch.empty(n, dtype=torch.int32, device=dev)
         cnt = torch.full((1,), -1, dtype=torch.int32, device=dev)
+        flags = torch.full((1,), -1, dtype=torch.int32, device=dev)
         L.check(lib.rta_diffuse_bounce_noalloc(C.byref(bvh.view), P._ptr(g.gpu_origin),
                                                P._ptr(g.gpu_direction), P._ptr(hits), n, seed,
                                                np.float32(1e-4), P._ptr(oo), P._ptr(od), P._ptr(om),
-                                               P._ptr(src), P._ptr(cnt), stream),
+                                               P._ptr(src), P._ptr(cnt), P._ptr(flags), stream),
                 "rta_diffuse_bounce_noalloc")
         torch.cuda.synchronize()
+        assert int(flags.item()) == 0   # no look-back wait gave up
         c = int(cnt.item())
         return (c, oo[: 3 * c].cpu().numpy(), od[: 3 * c].cpu().numpy(), om[:c].cpu().numpy(),
                 src[:c].cpu().numpy())
 
-    # two calls in a row, the second smaller than the first and with another seed
-    for (w, h), seed in (((320, 180), 3), ((160, 90), 4)):
+    # calls in a row, each smaller than the one before and with another seed;
+    # the last is one partial tile (< 1024 rays), so the look-back words the
+    # larger calls left beyond its range must not matter
+    for (w, h), seed in (((320, 180), 3), ((160, 90), 4), ((40, 20), 5)):
         g, hits = primary(w, h)
         want = with_frame_ctx(g, hits, w * h, seed)
         got = without_alloc(g, hits, w * h, seed)
         assert want[0] > 0 and got[0] == want[0]
         for a, b in zip(got[1:], want[1:]):
             np.testing.assert_array_equal(np.asarray(a).view(np.uint32), np.asarray(b).view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_noalloc_bounce_at_exactly_the_scratch_limit():
+    """RTA_BOUNCE_NOALLOC_MAX_RAYS rays, all misses: the call uses every
+    look-back word of the scratch and reports no bounce ray."""
+    torch = pytest.importorskip("torch")
+    from rta_gb300 import plugin as P
+    from rta_gb300 import scenes as S
+
+    lib = L.load()
+    dev = torch.device("cuda")
+    bvh = P.lbvh_constructor(morton_bits=30).build(P.cuda_ftl(S.terrain(8, 4, seed=1)))
+    n = L.BOUNCE_NOALLOC_MAX_RAYS
+    stream = P._stream()
+    rays = torch.zeros(3 * n, dtype=torch.float32, device=dev)
+    hits = torch.empty(4 * n, dtype=torch.float32, device=dev)
+    L.check(lib.rta_reset_intersections(P._ptr(hits), n, 1, stream), "reset")
+    oo = torch.empty(3 * n, dtype=torch.float32, device=dev)
+    od = torch.empty(3 * n, dtype=torch.float32, device=dev)
+    om = torch.empty(n, dtype=torch.float32, device=dev)
+    src = torch.empty(n, dtype=torch.int32, device=dev)
+    cnt = torch.full((1,), -1, dtype=torch.int32, device=dev)
+    flags = torch.full((1,), -1, dtype=torch.int32, device=dev)
+    L.check(lib.rta_diffuse_bounce_noalloc(C.byref(bvh.view), P._ptr(rays), P._ptr(rays), P._ptr(hits), n, 7,
+                                           np.float32(1e-4), P._ptr(oo), P._ptr(od), P._ptr(om), P._ptr(src),
+                                           P._ptr(cnt), P._ptr(flags), stream), "rta_diffuse_bounce_noalloc")
+    torch.cuda.synchronize()
+    assert int(cnt.item()) == 0 and int(flags.item()) == 0
