@@ -304,6 +304,14 @@ def learned_eval(args, dev):
         loss = model.train(epochs=4, batch=1 << 16, lr=2e-3)
         torch.cuda.synchronize()
         train_s = time.perf_counter() - t0    # 4 epochs of the forward/backward and Adam kernels
+        # the confidence margin is chosen on the last training scene's rays
+        # (seed 3, at most 2M of them): the network overrides the plain order
+        # only where it is at least that sure, and never where that costs
+        # work on the training scene
+        vidx = torch.arange(0, int(m.numel()), max(1, int(m.numel()) >> 21), device=dev)
+        nv = int(vidx.numel())
+        chosen = LR.choose_margin(model, bvh, o.view(-1, 3)[vidx].contiguous(), d.view(-1, 3)[vidx].contiguous(),
+                                  m[vidx].contiguous())
         bvh = ctor.build(P.cuda_ftl(make(4)))
         if fam == "terrain":
             o, d, m = _frame_rays(lib, bvh, S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), w=3200, h=1800), 4, dev)
@@ -347,6 +355,10 @@ def learned_eval(args, dev):
         out[fam] = {
             "train_samples": samples, "train_loss_before": loss0, "train_loss_after": loss,
             "train_s": train_s, "sample_s": sample_s, "train_epochs": 4, "eval_rays": nr,
+            "margin": chosen["margin"] if np.isfinite(chosen["margin"]) else "inf",
+            "margin_selection": {"scene": "training seed 3, every k-th ray", "rays": nv,
+                                 "plain_work_per_ray": chosen["plain_work_per_ray"],
+                                 "work_per_ray_by_margin": chosen["tried"]},
             "plain": {"nodes_per_ray": float(spn[0]), "tris_per_ray": float(spn[1]), "ms": tp,
                       "mrays_s": nr / (tp * 1e-3) / 1e6},
             "learned": {"nodes_per_ray": float(sln[0]), "tris_per_ray": float(sln[1]), "ms": tl,

@@ -91,8 +91,8 @@ int rta_lbvh_destroy(rta_lbvh_ctx *ctx);
  * n triangles; build() calls it when n grows, as buildCUDA does (lbvh.h:157-162). */
 int rta_lbvh_reserve(rta_lbvh_ctx *ctx, uint32_t n, int morton_bits);
 
-/* Radix digit width of the build's key sort: 8 (default), 10 or 11 bits per
- * pass.  The sorted order is the same for every width (a stable LSD sort);
+/* Radix digit width of the build's key sort: 8 (default), 9, 10 or 11 bits
+ * per pass.  The sorted order is the same for every width (a stable LSD sort);
  * wider digits take fewer passes.  The reference sorts with thrust
  * (sortMortonCodes, lbvh-kernels.cu:537-555), which picks its own width. */
 int rta_lbvh_set_digit_bits(rta_lbvh_ctx *ctx, int digit_bits);
@@ -108,6 +108,23 @@ int rta_lbvh_set_digit_bits(rta_lbvh_ctx *ctx, int digit_bits);
  *              input buffer and indexes with triangle_intersection::ref */
 int rta_lbvh_build(rta_lbvh_ctx *ctx, const void *tris, uint32_t n, int morton_bits,
                    void *tris_out, rta_stream_t stream);
+
+/* Per-pass build timing, as lbvh_constructor::buildCUDA prints it under -v
+ * (lbvh.h:172-204): with timing on, rta_lbvh_build records CUDA events on its
+ * stream between its passes, and rta_lbvh_pass_ms waits for the last build's
+ * end and writes the milliseconds of each pass, in this order:
+ *   0  triangle boxes, centroids and the scene box (initTriangles +
+ *      calculateVoxelBounds)
+ *   1  Morton codes and the sort's digit histograms (calculateMortonCodes2)
+ *   2  the key sort (sortMortonCodes)
+ *   3  Karras radix tree and parent links (buildTreeKarras)
+ *   4  node boxes, equal-code collapse and the Morton-ordered triangles
+ *      (buildBoundingBoxesKarras2 + invert_triangle_permutation)
+ * Invalid before a timed build.  The events end the overlap of consecutive
+ * launches at the pass borders, so a timed build is slightly slower. */
+#define RTA_LBVH_PASSES 5
+int rta_lbvh_set_timing(rta_lbvh_ctx *ctx, int on);
+int rta_lbvh_pass_ms(rta_lbvh_ctx *ctx, float *ms);
 
 /* the built tree: binary_lbvh::take_node_array / take_index_array (lbvh.h:207-208) */
 int rta_lbvh_get(const rta_lbvh_ctx *ctx, rta_lbvh *out);
@@ -264,6 +281,11 @@ int rta_order_destroy(rta_order_model *model);
 uint32_t rta_order_param_count(void);
 int rta_order_get_params(const rta_order_model *model, float *host_params);
 int rta_order_set_params(rta_order_model *model, const float *host_params);
+/* Confidence margin of rta_trace_learned (default 0): the network's choice is
+ * taken only where |logit| > margin, the plain nearer-first order elsewhere;
+ * FLT_MAX (or any margin no logit exceeds) gives the plain traversal. */
+int rta_order_set_margin(rta_order_model *model, float margin);
+int rta_order_get_margin(const rta_order_model *model, float *margin);
 
 /* Plain child-is closest-hit trace (as rta_trace with RTA_TRACE_CIS) that
  * also records every node where both children are hit and not culled, then
@@ -339,7 +361,7 @@ typedef struct rta_batch rta_batch;
 
 /* Launch parameters of a batch (chosen by rta_batch_autotune or set). */
 typedef struct rta_batch_params {
-    int digit_bits;     /* sort digit width: 8, 10 or 11 */
+    int digit_bits;     /* sort digit width: 8, 9, 10 or 11 */
     int fetch_idle;     /* a warp fetches rays once this many lanes are idle: 1..32 */
     int blocks_per_sm;  /* persistent trace blocks per SM, 0 = occupancy maximum */
     int stack;          /* traversal stack entries: 40 or 64 */

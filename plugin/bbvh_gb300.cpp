@@ -76,6 +76,22 @@ class lbvh_as : public basic_acceleration_structure<box_t, tri_t> {
         cudaMemcpy(ids.data(), view.index, 4 * (size_t)view.n, cudaMemcpyDeviceToHost);
         return ids;
     }
+    // mamo triangle dump in the layout of binary_bvh::dump_primitives
+    // (bbvh/bbvh.h:53-65): positions and normals of the Morton-ordered records
+    void dump_primitives(const std::string &filename) override
+    {
+        tri_t *t = canonical_triangle_ptr();
+        std::ofstream out(filename.c_str());
+        out << "tri\n" << view.n << "\n";
+        for (uint32_t i = 0; i < view.n; ++i) {
+            const tri_t &q = t[i];
+            out << i << " " << q.a.x << " " << q.a.y << " " << q.a.z << " " << q.b.x << " " << q.b.y << " " << q.b.z
+                << " " << q.c.x << " " << q.c.y << " " << q.c.z << " " << q.na.x << " " << q.na.y << " " << q.na.z
+                << " " << q.nb.x << " " << q.nb.y << " " << q.nb.z << " " << q.nc.x << " " << q.nc.y << " " << q.nc.z
+                << "\n";
+        }
+        free_canonical_triangles(t);
+    }
     // mamo dump in the layout of binary_bvh::dump_acceleration_structure (bbvh/bbvh.h:36-52)
     void dump_acceleration_structure(const std::string &filename) override
     {
@@ -113,7 +129,11 @@ class lbvh_ctor : public basic_acceleration_structure_constructor<box_t, tri_t> 
 
   public:
     int morton_bits;
-    explicit lbvh_ctor(int bits) : morton_bits(bits) { checked(rta_lbvh_create(&ctx), "rta_lbvh_create"); }
+    explicit lbvh_ctor(int bits) : morton_bits(bits)
+    {
+        checked(rta_lbvh_create(&ctx), "rta_lbvh_create");
+        if (cmd.verbose) checked(rta_lbvh_set_timing(ctx, 1), "rta_lbvh_set_timing");
+    }
     ~lbvh_ctor() override
     {
         rta_lbvh_destroy(ctx);
@@ -132,16 +152,31 @@ class lbvh_ctor : public basic_acceleration_structure_constructor<box_t, tri_t> 
             }
             cap = n;
         }
-        wall_time_timer wtt;
-        wtt.start();
+        if (cmd.verbose) {
+            std::cout << "Triangles: " << n << std::endl;
+            std::cout << "Building BVH on GPU..." << std::endl;
+        }
         checked(rta_lbvh_build(ctx, tris->triangle, n, morton_bits, sorted, nullptr), "rta_lbvh_build");
         rta_lbvh v;
         checked(rta_lbvh_get(ctx, &v), "rta_lbvh_get");
         if (cmd.verbose) {
+            // the per-pass report of lbvh_constructor::buildCUDA (lbvh.h:172-204);
+            // the scene box is folded into the first pass and the triangle
+            // permutation into the last
+            float ms[RTA_LBVH_PASSES];
+            checked(rta_lbvh_pass_ms(ctx, ms), "rta_lbvh_pass_ms");
             uint32_t flags = 0;
             checked(rta_lbvh_status(&v, nullptr, &flags), "rta_lbvh_status");
-            std::cout << "lbvh of " << n << " triangles built in " << wtt.look() << " ms (flags " << flags
-                      << ")" << std::endl;
+            std::cout << "=========================================================" << std::endl;
+            std::cout << "Time for initializing Triangles and Voxel Bounds: " << ms[0] << " ms" << std::endl;
+            std::cout << "Time for calculating Morton Codes: " << ms[1] << " ms" << std::endl;
+            std::cout << "Time for sorting Morton Codes: " << ms[2] << " ms" << std::endl;
+            std::cout << "Time for tree construction: " << ms[3] << " ms" << std::endl;
+            std::cout << "Time for building the bounding boxes and permuting the triangles: " << ms[4] << " ms"
+                      << std::endl;
+            std::cout << "BVH finished. Total time: " << ms[0] + ms[1] + ms[2] + ms[3] + ms[4] << " ms (device flags "
+                      << flags << ")" << std::endl;
+            std::cout << "=========================================================" << std::endl;
         }
         return new lbvh_as(v, sorted);
     }
@@ -198,6 +233,27 @@ class shirley : public cuda::cam_ray_generator_shirley {
         cudaDeviceSynchronize();
     }
     std::string identification() override { return "cuda shirley ray generator (gb300)"; }
+    // mamo ray dump in the layout of cam_ray_generator_shirley::dump_rays
+    // (librta/raytrav.h:353-366), of the rays on the device (the CPU-side
+    // ray image the reference's CUDA generator inherits is never filled)
+    void dump_rays(const std::string &filename) override
+    {
+        const size_t n = (size_t)w * h;
+        std::vector<float> o(3 * n), d(3 * n), m(n);
+        cudaMemcpy(o.data(), gpu_origin, 12 * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(d.data(), gpu_direction, 12 * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(m.data(), gpu_maxt, 4 * n, cudaMemcpyDeviceToHost);
+        std::ofstream out(filename.c_str());
+        const int iw = (int)w, ih = (int)h;
+        out << "ray\n" << iw << " " << ih << "\n";
+        for (int y = 0; y < ih; ++y)
+            for (int x = 0; x < iw; ++x) {
+                const size_t i = (size_t)y * iw + x;
+                out << y * iw + x << " " << 2 << " " << o[3 * i] << " " << o[3 * i + 1] << " " << o[3 * i + 2] << " "
+                    << d[3 * i] << " " << d[3 * i + 1] << " " << d[3 * i + 2] << " "
+                    << "0 " << m[i] << "\n";
+            }
+    }
 };
 
 } // namespace gb300

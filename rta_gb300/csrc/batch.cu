@@ -186,7 +186,7 @@ static int batch_sms()
 
 static bool valid_params(const rta_batch_params &p)
 {
-    return (p.digit_bits == 8 || p.digit_bits == 10 || p.digit_bits == 11) && p.fetch_idle >= 1 &&
+    return (p.digit_bits >= 8 && p.digit_bits <= 11) && p.fetch_idle >= 1 &&
            p.fetch_idle <= 32 && p.blocks_per_sm >= 0 && p.blocks_per_sm <= 64 && (p.stack == 40 || p.stack == 64);
 }
 
@@ -244,7 +244,7 @@ static void free_batch(rta_batch *b)
 static size_t batch_status_words(int key_bits)
 {
     size_t w = 0;
-    for (int d : {8, 10, 11}) w = std::max(w, (size_t)sort_passes(key_bits, d) << d);
+    for (int d : {8, 9, 10, 11}) w = std::max(w, (size_t)sort_passes(key_bits, d) << d);
     return w;
 }
 
@@ -277,6 +277,10 @@ static int batch_build_impl(rta_batch *b, const void *tris, cudaStream_t s)
     uint64_t *ks = nullptr;
     uint32_t *vs = nullptr;
     switch (db) {
+    case 9:
+        rc = sort_passes_launch<uint64_t, 9>(b->keys0, b->keys1, b->vals0, b->vals1, n, passes, hdr, tstat,
+                                             b->status, b->codes, kCodeMask30, s, &ks, &vs);
+        break;
     case 10:
         rc = sort_passes_launch<uint64_t, 10>(b->keys0, b->keys1, b->vals0, b->vals1, n, passes, hdr, tstat,
                                               b->status, b->codes, kCodeMask30, s, &ks, &vs);
@@ -715,7 +719,7 @@ int rta_batch_autotune(rta_batch *b, const void *tris, const float *orig, const 
     };
     const int max_bps = batch_trace_max_blocks_per_sm(40);
     const std::vector<std::vector<int>> cand = {
-        {8, 10, 11}, {4, 8, 12, 16, 24}, {0, std::max(1, max_bps / 2), std::max(1, (3 * max_bps) / 4)}, {40, 64}};
+        {8, 9, 10, 11}, {4, 8, 12, 16, 24}, {0, std::max(1, max_bps / 2), std::max(1, (3 * max_bps) / 4)}, {40, 64}};
     rta_batch_params best = b->params;
     if (sort_passes(30 + (int)b->mesh_bits, best.digit_bits) > kMaxPasses) best.digit_bits = 8;
     float best_t = 0.f;

@@ -276,7 +276,7 @@ using namespace rta;
 struct rta_lbvh_ctx {
     uint32_t cap = 0;
     int bits = 0;
-    int digit_bits = 8;   // radix digit width of the sort (8, 10 or 11)
+    int digit_bits = 8;   // radix digit width of the sort (8 to 11)
     // device buffers
     void *keys0 = nullptr, *keys1 = nullptr;
     uint32_t *vals0 = nullptr, *vals1 = nullptr;
@@ -300,6 +300,10 @@ struct rta_lbvh_ctx {
     // recorded on the build's stream after each build's last kernel: work on
     // other streams that reads the tree waits for it (rta_lbvh::ready)
     cudaEvent_t built = nullptr;
+    // per-pass timing (rta_lbvh_set_timing): events before the first pass
+    // and after each of the RTA_LBVH_PASSES passes of the last build
+    bool timing = false, timed = false;
+    cudaEvent_t pass_ev[RTA_LBVH_PASSES + 1] = {};
 };
 
 static int bounds_blocks(uint32_t n)
@@ -309,14 +313,14 @@ static int bounds_blocks(uint32_t n)
     return want < cap ? (want > 0 ? want : 1) : cap;
 }
 
-static bool valid_digit_bits(int b) { return b == 8 || b == 10 || b == 11; }
+static bool valid_digit_bits(int b) { return b >= 8 && b <= 11; }
 
 
 // tile status words per tile, the most any supported digit width needs
 static size_t status_words_per_tile(int key_bits)
 {
     size_t w = 0;
-    for (int b : {8, 10, 11}) {
+    for (int b : {8, 9, 10, 11}) {
         size_t v = (size_t)sort_passes(key_bits, b) << b;
         if (v > w) w = v;
     }
@@ -329,11 +333,13 @@ static void free_ctx(rta_lbvh_ctx *c)
                     c->nodes, c->root,  c->parents, c->counters, c->tris, c->status,  c->rbox};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    const int db = c->digit_bits;
-    cudaEvent_t built = c->built;
-    *c = rta_lbvh_ctx();
-    c->digit_bits = db;
-    c->built = built;
+    // the settings and events outlive the buffers
+    rta_lbvh_ctx keep;
+    keep.digit_bits = c->digit_bits;
+    keep.built = c->built;
+    keep.timing = c->timing;
+    for (int k = 0; k <= RTA_LBVH_PASSES; ++k) keep.pass_ev[k] = c->pass_ev[k];
+    *c = keep;
 }
 
 template <typename Key>
@@ -345,6 +351,10 @@ static int sort_keys(rta_lbvh_ctx *c, uint32_t n, int passes, SortScratchHeader 
     int rc;
     Key *k0 = (Key *)c->keys0, *k1 = (Key *)c->keys1;
     switch (c->digit_bits) {
+    case 9:
+        rc = sort_passes_launch<Key, 9>(k0, k1, c->vals0, c->vals1, n, passes, hdr, tstat, c->status, nullptr,
+                                        0u, s, &ks, &vs, true);
+        break;
     case 10:
         rc = sort_passes_launch<Key, 10>(k0, k1, c->vals0, c->vals1, n, passes, hdr, tstat, c->status, nullptr,
                                          0u, s, &ks, &vs, true);
@@ -380,6 +390,8 @@ int rta_lbvh_destroy(rta_lbvh_ctx *ctx)
     if (!ctx) return RTA_ERR_INVALID;
     free_ctx(ctx);
     if (ctx->built) cudaEventDestroy(ctx->built);
+    for (cudaEvent_t e : ctx->pass_ev)
+        if (e) cudaEventDestroy(e);
     delete ctx;
     return RTA_OK;
 }
@@ -436,12 +448,21 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
     uint32_t *tstat = reinterpret_cast<uint32_t *>(c->scratch + sizeof(SortScratchHeader));
     const size_t used = sizeof(SortScratchHeader) + ((size_t)passes << db) * tiles * 4;
     RTA_CUDA_TRY(cudaMemsetAsync(c->scratch, 0, used, s));
+    // per-pass events (only with timing on; they end the launches' overlap
+    // at the pass borders)
+    auto mark = [&](int k) -> int {
+        if (c->timing) RTA_CUDA_TRY(cudaEventRecord(c->pass_ev[k], s));
+        return RTA_OK;
+    };
+    c->timed = false;
+    if ((rc = mark(0))) return rc;
 
     const float *tin = static_cast<const float *>(tris);
     const int bb = bounds_blocks(n);
     k_bounds<<<bb, kBoundsThreads, 0, s>>>(tin, n, c->cent, c->partial, c->state, c->status,
                                            bits == 63 ? 2097152.0f : 1024.0f);
     if ((rc = check_launch("k_bounds"))) return rc;
+    if ((rc = mark(1))) return rc;
     const int eb = (int)((n + 255) / 256);
     const int mb = eb < num_sms() * 8 ? eb : num_sms() * 8;
     const uint32_t gmask = bits == 63 ? 0x1fffffu : 0x3ffu;
@@ -461,15 +482,18 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
                                          (const float *)c->cent, n, (uint32_t *)c->keys0,
                                          (const BuildState *)c->state, hdr, c->status, passes, db, gmask));
 
+    if ((rc = mark(2))) return rc;
     rc = bits == 63 ? sort_keys<uint64_t>(c, n, passes, hdr, tstat, s)
                     : sort_keys<uint32_t>(c, n, passes, hdr, tstat, s);
     if (rc) return rc;
+    if ((rc = mark(3))) return rc;
     RTA_CUDA_TRY(bits == 63 ? launch_pdl(true, k_karras<uint64_t>, dim3(eb), dim3(256), 0, s,
                                          (const uint64_t *)c->codes, (const uint32_t *)c->index, n, c->nodes,
                                          c->parents, c->counters, tin, (float *)tris_out)
                             : launch_pdl(true, k_karras<uint32_t>, dim3(eb), dim3(256), 0, s,
                                          (const uint32_t *)c->codes, (const uint32_t *)c->index, n, c->nodes,
                                          c->parents, c->counters, tin, (float *)tris_out));
+    if ((rc = mark(4))) return rc;
     const uint32_t cap = n > 1 ? n - 1 : 1;
     rc = bits == 63 ? refit_launch<uint64_t, false>((const uint64_t *)c->codes, n, nullptr, nullptr, tin, c->index,
                                                     c->nodes, c->parents, c->tris, c->root, c->rbox, c->counters,
@@ -480,10 +504,31 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
                                                     cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s,
                                                     true);
     if (rc) return rc;
+    if ((rc = mark(5))) return rc;
+    c->timed = c->timing;
     if (!c->built) RTA_CUDA_TRY(cudaEventCreateWithFlags(&c->built, cudaEventDisableTiming));
     RTA_CUDA_TRY(cudaEventRecord(c->built, s));
     c->n = n;
     c->last_bits = bits;
+    return RTA_OK;
+}
+
+int rta_lbvh_set_timing(rta_lbvh_ctx *c, int on)
+{
+    if (!c) return RTA_ERR_INVALID;
+    if (on && !c->pass_ev[0])
+        for (cudaEvent_t &e : c->pass_ev) RTA_CUDA_TRY(cudaEventCreate(&e));
+    c->timing = on != 0;
+    c->timed = false;
+    return RTA_OK;
+}
+
+int rta_lbvh_pass_ms(rta_lbvh_ctx *c, float *ms)
+{
+    if (!c || !ms || !c->timed) return RTA_ERR_INVALID;
+    RTA_CUDA_TRY(cudaEventSynchronize(c->pass_ev[RTA_LBVH_PASSES]));
+    for (int k = 0; k < RTA_LBVH_PASSES; ++k)
+        RTA_CUDA_TRY(cudaEventElapsedTime(&ms[k], c->pass_ev[k], c->pass_ev[k + 1]));
     return RTA_OK;
 }
 

@@ -18,12 +18,16 @@ namespace rta {
 constexpr int kTriFloats = 26;         // cuda::simple_triangle = 104 bytes
 constexpr int kBoundsThreads = 256;
 constexpr int kSortThreads = 256;      // 8 warps
-constexpr int kSortItems = 16;
-// blocks per SM the onesweep kernel must fit in registers: 3 caps the 64-bit
-// key passes at 80 registers (from 128: 2 blocks per SM) at a few spilled
-// bytes, 1.5 % off the 4M build; 12 or 8 keys per thread measured slower
+#ifndef RTA_SORT_ITEMS
+#define RTA_SORT_ITEMS 16
+#endif
+constexpr int kSortItems = RTA_SORT_ITEMS;   // keys per thread
+// blocks per SM the onesweep kernel must fit in registers.  With the
+// lane-mask ranking, 2 (no spills) measured faster than 3 (80 registers,
+// 56-120 spilled bytes): 1M 30-bit build 0.249 -> 0.234 ms, 4M 63-bit
+// 0.996 -> 0.980 ms; 12, 24 or 32 keys per thread were not faster
 #ifndef RTA_SORT_MIN_BLOCKS
-#define RTA_SORT_MIN_BLOCKS 3
+#define RTA_SORT_MIN_BLOCKS 2
 #endif
 constexpr int kSortTile = kSortThreads * kSortItems;   // 4096 keys per tile
 constexpr int kMaxDigitBits = 11;
@@ -110,8 +114,10 @@ __device__ __forceinline__ uint64_t morton_code(const float c[3], const float lo
 // one onesweep LSD radix pass                                                 //
 // ------------------------------------------------------------------------- //
 //
-// A tile of 4096 keys per block: warp-level stable ranking with one ballot
-// per digit bit, per-warp digit counters in shared memory, decoupled
+// A tile of 4096 keys per block: warp-level stable ranking by lane masks
+// (each lane ORs its bit into a shared word of its digit; the word then names
+// the lanes with equal digits, whatever the digit width), per-warp digit
+// counters in shared memory, decoupled
 // look-back across tiles for the per-digit prefix (Merrill & Garland's
 // single-pass scan as used by Adinets & Merrill's Onesweep), a shared-memory
 // staging of the tile in digit order, and coalesced runs out to global
@@ -126,8 +132,15 @@ struct SortSmem {
     uint32_t glob[kRadix];
     uint32_t scan_tmp[kSortThreads / 32];
     uint32_t tile;
-    Key keys[kSortTile];
-    uint32_t vals[kSortTile];
+    // the ranking's lane masks are dead once the tile is ranked, the staging
+    // area is live only afterwards: they share the space
+    union {
+        uint32_t match[kSortThreads / 32][kRadix];   // per warp and digit: lanes holding that digit
+        struct {
+            Key keys[kSortTile];
+            uint32_t vals[kSortTile];
+        } stage;
+    } u;
 };
 
 // block-wide exclusive scan of one value per thread (256 threads)
@@ -185,7 +198,10 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
 
     if (tid == 0) S.tile = atomicAdd(tile_ctr, 1u);
-    for (int j = tid; j < (kSortThreads / 32) * kRadix; j += kSortThreads) (&S.whist[0][0])[j] = 0;
+    for (int j = tid; j < (kSortThreads / 32) * kRadix; j += kSortThreads) {
+        (&S.whist[0][0])[j] = 0;
+        (&S.u.match[0][0])[j] = 0;
+    }
     __syncthreads();
     const uint32_t tile = S.tile;
     const uint32_t base = tile * kSortTile;
@@ -194,34 +210,37 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
     Key k[kSortItems];
     uint32_t v[kSortItems];
     uint32_t rank[kSortItems];
-    uint32_t dig[kSortItems];
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
         uint32_t idx = wbase + i * 32 + lane;
         bool ok = idx < n;
         k[i] = ok ? kin[idx] : (Key)~(Key)0;
         v[i] = ok ? (vin ? vin[idx] : idx) : 0u;
-        dig[i] = (uint32_t)(k[i] >> shift) & kDigitMask;
     }
-    const uint32_t lt_mask = (1u << lane) - 1u;
+    // Stable rank of each key among the warp's keys of its digit, in (item,
+    // lane) order: the lanes OR their bit into the digit's mask word; the
+    // highest lane of a mask is its leader, adds the lane count to the warp's
+    // digit counter and clears the word; the others take the old counter
+    // from it.  The warp's keys are consecutive in the input (item-major),
+    // so the order is the input order.
+    const uint32_t lane_bit = 1u << lane;
+    const uint32_t le_mask = lane_bit | (lane_bit - 1u);
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
-        const uint32_t d = dig[i];
-        uint32_t peers = 0xffffffffu;
-#pragma unroll
-        for (int b = 0; b < BITS; ++b) {
-            uint32_t bal = __ballot_sync(0xffffffffu, (d >> b) & 1u);
-            peers &= ((d >> b) & 1u) ? bal : ~bal;
-        }
-        const int leader = __ffs(peers) - 1;
-        uint32_t prev = 0;
-        if (lane == leader) {
-            prev = S.whist[w][d];
-            S.whist[w][d] = prev + __popc(peers);
-        }
+        const uint32_t d = (uint32_t)(k[i] >> shift) & kDigitMask;
+        uint32_t *m = &S.u.match[w][d];
+        atomicOr(m, lane_bit);
         __syncwarp();
-        prev = __shfl_sync(0xffffffffu, prev, leader);
-        rank[i] = prev + __popc(peers & lt_mask);
+        const uint32_t peers = *m;
+        const int leader = 31 - __clz(peers);
+        const uint32_t upto = __popc(peers & le_mask);   // 1-based position among the peers
+        uint32_t off = 0;
+        if (lane == leader) off = atomicAdd(&S.whist[w][d], upto);   // the leader's upto = all peers
+        off = __shfl_sync(0xffffffffu, off, leader);
+        // every lane has read the mask (its value fed the shuffle above)
+        if (lane == leader) *m = 0u;
+        __syncwarp();
+        rank[i] = off + upto - 1u;
     }
     __syncthreads();
 
@@ -275,16 +294,17 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
 
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
-        uint32_t pos = S.digit_start[dig[i]] + S.whist[w][dig[i]] + rank[i];
-        S.keys[pos] = k[i];
-        S.vals[pos] = v[i];
+        const uint32_t d = (uint32_t)(k[i] >> shift) & kDigitMask;
+        uint32_t pos = S.digit_start[d] + S.whist[w][d] + rank[i];
+        S.u.stage.keys[pos] = k[i];
+        S.u.stage.vals[pos] = v[i];
     }
     __syncthreads();
     for (uint32_t j = tid; j < valid; j += kSortThreads) {
-        Key key = S.keys[j];
+        Key key = S.u.stage.keys[j];
         uint32_t dst = S.glob[(uint32_t)(key >> shift) & kDigitMask] + j;
         kout[dst] = key;
-        vout[dst] = S.vals[j];
+        vout[dst] = S.u.stage.vals[j];
         if (code_out) code_out[dst] = (uint32_t)key & code_mask;
     }
 }

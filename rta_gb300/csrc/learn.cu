@@ -327,6 +327,7 @@ using namespace rta;
 
 struct rta_order_model {
     uint32_t cap = 0;
+    float margin = 0.0f;   // host copy of MlpWeights::margin
     Sample *samples = nullptr;
     uint32_t *counters = nullptr;   // [0] samples written, [1] trace queue
     float *params = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *loss = nullptr;
@@ -409,6 +410,21 @@ int rta_order_set_params(rta_order_model *c, const float *host_params)
     k_publish<<<1, 256>>>(c->params, c->weights);
     RTA_CUDA_TRY(cudaGetLastError());
     RTA_CUDA_TRY(cudaDeviceSynchronize());
+    return RTA_OK;
+}
+
+int rta_order_set_margin(rta_order_model *c, float margin)
+{
+    if (!c || !(margin >= 0.0f)) return RTA_ERR_INVALID;
+    RTA_CUDA_TRY(cudaMemcpy(&c->weights->margin, &margin, 4, cudaMemcpyHostToDevice));
+    c->margin = margin;
+    return RTA_OK;
+}
+
+int rta_order_get_margin(const rta_order_model *c, float *margin)
+{
+    if (!c || !margin) return RTA_ERR_INVALID;
+    *margin = c->margin;
     return RTA_OK;
 }
 

@@ -30,7 +30,8 @@ struct MlpWeights {
     float b1[kMlpHidden];
     float b2[kMlpHidden];
     float b3;
-    float pad[3];
+    float margin;   // the network overrides the plain order only where |logit| > margin
+    float pad[2];
 };
 
 // one decision of the plain traversal, as recorded for training: the

@@ -967,6 +967,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
     uint32_t hint_ref = 0xffffffffu;   // HINT: Morton position of the known hit
     bool parked = false;        // LEARNED: waiting for the warp's next network pass
     uint32_t pq_l = 0, pq_r = 0;   // child links of the parked decision
+    bool pq_plain = false;         // the plain rule's choice there: left first
     uint32_t px[kMlpIn / 2];    // its features, packed bf16 pairs
 
     for (;;) {
@@ -1096,6 +1097,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
                     parked = true;
                     pq_l = nd.q3.x;
                     pq_r = nd.q3.y;
+                    pq_plain = tnl <= tnr;
                 }
                 const uint32_t pm = __ballot_sync(0xffffffffu, parked);
                 if (pm && (__popc(pm) >= kParkMin || pm == __ballot_sync(0xffffffffu, active))) {
@@ -1113,7 +1115,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_learn(LearnArgs L)
                             overflow = true;
                             done = true;
                         } else {
-                            const bool lf = logit > 0.0f;
+                            // a confident network decides; below the margin
+                            // the plain nearer-first rule does
+                            const bool lf = fabsf(logit) > sw.margin ? logit > 0.0f : pq_plain;
                             const uint32_t far = lf ? pq_r : pq_l;
                             const uint32_t d1 = depth + 1u < 63u ? depth + 1u : 63u;
                             stack[++sp] = is_leaf(far) ? far : (far | (d1 << kCountShift));

@@ -63,6 +63,15 @@ class OrderModel:
         p = np.ascontiguousarray(p, np.float32)
         L.check(self.lib.rta_order_set_params(self.handle, p.ctypes.data_as(C.c_void_p)), "set_params")
 
+    def set_margin(self, margin: float) -> None:
+        """The network overrides the plain order only where |logit| > margin."""
+        L.check(self.lib.rta_order_set_margin(self.handle, np.float32(margin)), "rta_order_set_margin")
+
+    def margin(self) -> float:
+        m = C.c_float(0)
+        L.check(self.lib.rta_order_get_margin(self.handle, C.byref(m)), "rta_order_get_margin")
+        return float(m.value)
+
     # ---- samples ----
     def sample(self, bvh, orig, dirs, maxt, nrays=None, d_nrays=None) -> torch.Tensor:
         """Plain trace that records decisions; returns the hits (device)."""
@@ -148,6 +157,32 @@ def work_per_ray(stats: torch.Tensor) -> float:
     """Mean nodes + triangles tested per ray."""
     s = stats.view(-1, 2).to(torch.float64)
     return float(s.sum(1).mean())
+
+
+MARGINS = (0.0, 0.5, 1.0, 2.0, 4.0, 8.0, 16.0, float("inf"))
+
+
+def choose_margin(model: OrderModel, bvh, orig, dirs, maxt, candidates=MARGINS) -> dict:
+    """Sets the confidence margin (rta_order_set_margin) that gives the least
+    mean nodes + triangles tested per ray on the given rays, which should be
+    rays of the training scenes.  An infinite margin is the plain order, so
+    the choice never does worse than plain on these rays; of equal results
+    the larger margin (closer to plain) wins."""
+    _, sp = plain_trace(bvh, orig, dirs, maxt, stats=True)
+    plain = work_per_ray(sp)
+    best_m, best_w, table = float("inf"), plain, {}
+    for mg in candidates:
+        if mg == float("inf"):
+            table["inf"] = plain
+            continue
+        model.set_margin(mg)
+        _, sl = model.trace(bvh, orig, dirs, maxt, stats=True)
+        w = work_per_ray(sl)
+        table[repr(mg)] = w
+        if w < best_w or (w == best_w and mg > best_m):
+            best_m, best_w = mg, w
+    model.set_margin(3.0e38 if best_m == float("inf") else best_m)
+    return {"margin": best_m, "work_per_ray": best_w, "plain_work_per_ray": plain, "tried": table}
 
 
 def keep_for_scene(model: OrderModel, bvh, orig, dirs, maxt) -> dict:

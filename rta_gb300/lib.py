@@ -17,16 +17,19 @@ OK = 0
 ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_NOMEM = -1, -2, -3, -4
 DEV_STACK_OVERFLOW, DEV_SPIN_TIMEOUT, DEV_QUANT_WRAP, DEV_ZERO_EXTENT, DEV_ITER_LIMIT, DEV_BAD_LINK = 1, 2, 4, 8, 16, 32
 TRACE_CIS, TRACE_DIS, TRACE_SHADOW, TRACE_AILA, TRACE_STATS = 0, 1, 2, 4, 8
+LBVH_PASSES = 5
 
 # every symbol include/rta_gb300.h declares
 SYMBOLS = [
     "rta_last_error", "rta_lbvh_max_triangles", "rta_lbvh_create", "rta_lbvh_destroy",
-    "rta_lbvh_reserve", "rta_lbvh_set_digit_bits", "rta_lbvh_build", "rta_lbvh_get", "rta_lbvh_status", "rta_lbvh_to_2f4",
+    "rta_lbvh_reserve", "rta_lbvh_set_digit_bits", "rta_lbvh_build", "rta_lbvh_set_timing", "rta_lbvh_pass_ms",
+    "rta_lbvh_get", "rta_lbvh_status", "rta_lbvh_to_2f4",
     "rta_trace", "rta_setup_shirley_rays", "rta_reset_intersections", "rta_frame_create",
     "rta_frame_destroy", "rta_frame_get", "rta_diffuse_bounce", "rta_frame_run",
     "rta_frame_status", "rta_frame_set_timing", "rta_frame_trace_ms", "rta_host_frames_create", "rta_host_frames_destroy", "rta_host_frames_run",
     "rta_diffuse_bounce_noalloc", "rta_order_create", "rta_order_destroy",
-    "rta_order_param_count", "rta_order_get_params", "rta_order_set_params", "rta_order_sample",
+    "rta_order_param_count", "rta_order_get_params", "rta_order_set_params", "rta_order_set_margin",
+    "rta_order_get_margin", "rta_order_sample",
     "rta_order_sample_count", "rta_order_clear_samples", "rta_order_samples", "rta_order_gradient",
     "rta_order_train", "rta_trace_learned", "rta_trace_ideal_order",
     "rta_shade_lambert", "rta_batch_create", "rta_batch_destroy", "rta_batch_set_meshes", "rta_batch_build", "rta_batch_trace",
@@ -85,6 +88,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_lbvh_reserve.argtypes = [vp, u32, i32]
     L.rta_lbvh_set_digit_bits.argtypes = [vp, i32]
     L.rta_lbvh_build.argtypes = [vp, vp, u32, i32, vp, vp]
+    L.rta_lbvh_set_timing.argtypes = [vp, i32]
+    L.rta_lbvh_pass_ms.argtypes = [vp, P(f32)]
     L.rta_lbvh_get.argtypes = [vp, P(LbvhView)]
     L.rta_lbvh_status.argtypes = [P(LbvhView), vp, P(u32)]
     L.rta_lbvh_to_2f4.argtypes = [P(LbvhView), vp, vp]
@@ -107,6 +112,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_order_param_count.restype = u32
     L.rta_order_get_params.argtypes = [vp, vp]
     L.rta_order_set_params.argtypes = [vp, vp]
+    L.rta_order_set_margin.argtypes = [vp, f32]
+    L.rta_order_get_margin.argtypes = [vp, P(f32)]
     L.rta_order_sample.argtypes = [vp, P(LbvhView), vp, vp, vp, u32, vp, vp, vp]
     L.rta_order_sample_count.argtypes = [vp, P(u32)]
     L.rta_order_clear_samples.argtypes = [vp]

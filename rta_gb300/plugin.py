@@ -112,28 +112,71 @@ class binary_lbvh:
 
     def dump_acceleration_structure(self, filename: str) -> None:
         """mamo text dump, the format of binary_bvh::dump_acceleration_structure
-        (bbvh/bbvh.h:36-52)."""
-        nodes = self.node_data_2f4()
-        bits = nodes.view(np.uint32)
+        (bbvh/bbvh.h:36-52), of the tree in the 2F4 node numbering."""
         with open(filename, "w") as f:
-            f.write(f"bvh\n{nodes.shape[0]}\n")
-            for i in range(nodes.shape[0]):
-                w0, w1 = int(bits[i, 0]), int(bits[i, 1])
-                inner = (w0 & 1) == 1
-                box = " ".join(f"{v:g}" for v in nodes[i, 2:8])
-                if inner:
-                    f.write(f"{i} I {box} 0 {w0 >> 1} {w1}\n")
-                else:
-                    el = w0 >> 1
-                    f.write(f"{i} L {box} {el}" + "".join(f" {w1 + j}" for j in range(el)) + "\n")
+            f.write(format_bvh_dump(self.node_data_2f4()))
 
     def dump_primitives(self, filename: str) -> None:
-        """mamo triangle dump (bbvh/bbvh.h:53-65)."""
-        t = self.canonical_triangle_ptr()
+        """mamo triangle dump (bbvh/bbvh.h:53-65) of the Morton-ordered records."""
         with open(filename, "w") as f:
-            f.write(f"tri\n{t.shape[0]}\n")
-            for i in range(t.shape[0]):
-                f.write(f"{i} " + " ".join(f"{v:g}" for v in t[i, 0:18]) + "\n")
+            f.write(format_tri_dump(self.canonical_triangle_ptr()))
+
+
+# --------------------------------------------------------------------------- #
+# mamo text dumps: the reference writes them through std::ostream with its    #
+# default float format (%g, 6 significant digits); these give the same text   #
+# --------------------------------------------------------------------------- #
+
+def _fmt(v) -> str:
+    """One float as `std::ostream << float` prints it by default: %g of the
+    value widened to double, "inf" / "-inf", and "nan" / "-nan" by the sign
+    bit (as glibc prints NaNs)."""
+    x = float(v)
+    if x != x:
+        return "-nan" if np.signbit(np.float32(v)) else "nan"
+    return f"{x:g}"
+
+
+def format_bvh_dump(nodes_2f4: np.ndarray) -> str:
+    """binary_bvh::dump_acceleration_structure (bbvh/bbvh.h:36-52) of nodes in
+    the 2F4 layout, (m, 8) float32: `i I|L box...` then `axis left right`
+    for an inner node (the split axis of an LBVH node is 0, as bbvh_node's),
+    `count tri tri+1 ...` for a leaf."""
+    nodes = np.ascontiguousarray(nodes_2f4, np.float32).reshape(-1, 8)
+    bits = nodes.view(np.uint32)
+    out = [f"bvh\n{nodes.shape[0]}\n"]
+    for i in range(nodes.shape[0]):
+        w0, w1 = int(bits[i, 0]), int(bits[i, 1])
+        box = " ".join(_fmt(v) for v in nodes[i, 2:8])
+        if w0 & 1:
+            out.append(f"{i} I {box} 0 {w0 >> 1} {w1}\n")
+        else:
+            el = w0 >> 1
+            out.append(f"{i} L {box} {el}" + "".join(f" {(w1 + j) & 0xFFFFFFFF}" for j in range(el)) + "\n")
+    return "".join(out)
+
+
+def format_tri_dump(tris: np.ndarray) -> str:
+    """binary_bvh::dump_primitives (bbvh/bbvh.h:53-65): index, positions a, b, c
+    and normals na, nb, nc of each 104-byte record."""
+    t = np.ascontiguousarray(tris, np.float32).reshape(-1, TRI_FLOATS)
+    out = [f"tri\n{t.shape[0]}\n"]
+    for i in range(t.shape[0]):
+        out.append(f"{i} " + " ".join(_fmt(v) for v in t[i, 0:18]) + "\n")
+    return "".join(out)
+
+
+def format_ray_dump(orig, dirs, maxt, w: int, h: int) -> str:
+    """cam_ray_generator_shirley::dump_rays (librta/raytrav.h:353-366): per ray
+    `y*w+x 2 origin direction 0 max_t`."""
+    o = np.asarray(orig, np.float32).reshape(-1, 3)
+    d = np.asarray(dirs, np.float32).reshape(-1, 3)
+    m = np.asarray(maxt, np.float32).reshape(-1)
+    out = [f"ray\n{int(w)} {int(h)}\n"]
+    for i in range(int(w) * int(h)):
+        out.append(f"{i} 2 {_fmt(o[i, 0])} {_fmt(o[i, 1])} {_fmt(o[i, 2])} "
+                   f"{_fmt(d[i, 0])} {_fmt(d[i, 1])} {_fmt(d[i, 2])} 0 {_fmt(m[i])}\n")
+    return "".join(out)
 
 
 class _DevArray:
@@ -212,6 +255,13 @@ class gpu_ray_generator:
 
     def res_x(self):
         return self.w
+
+    def dump_rays(self, filename: str) -> None:
+        """mamo ray dump (librta/raytrav.h:353-366) of the rays on the device."""
+        torch.cuda.synchronize()
+        with open(filename, "w") as f:
+            f.write(format_ray_dump(self.gpu_origin.cpu().numpy(), self.gpu_direction.cpu().numpy(),
+                                    self.gpu_maxt.cpu().numpy(), self.w, self.h))
 
     def res_y(self):
         return self.h

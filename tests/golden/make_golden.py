@@ -18,8 +18,16 @@ and this script feeds them seeded inputs and stores inputs and outputs:
                        original triangle id.
 * ``terrain_trace.npz`` a 64x32-quad terrain seen by a 160x90 camera: hits of
                        the CIS and DIS kernels.
+* ``mamo_dumps.npz``   the reference's own mamo text dumps
+                       (binary_bvh::dump_acceleration_structure / ::dump_primitives,
+                       bbvh/bbvh.h:36-65; cam_ray_generator_shirley::dump_rays,
+                       librta/raytrav.h:353-366) of a 256-triangle terrain's
+                       reference LBVH, its triangles and a 16x4 ray image, with
+                       nodes, triangles and rays of special values appended
+                       (-0, +-inf, +-NaN, subnormal, integral and large values).
 
 Run from the repository root:  python tests/golden/make_golden.py
+(``python tests/golden/make_golden.py dumps`` remakes mamo_dumps.npz alone)
 """
 from __future__ import annotations
 
@@ -139,9 +147,64 @@ def small_cases():
     return {k: np.asarray(v, np.float32) for k, v in cases.items()}
 
 
+SPECIALS = np.array([-0.0, np.inf, -np.inf, np.nan, -np.nan, 1e-7, 123456789.0, 0.1, 3.0, 1e20, 5e-39,
+                     -2.5, 65536.0, 1.0 / 3.0], np.float32)
+SPECIALS[4] = np.float32(np.copysign(np.float32(np.nan), -1.0))   # NaN with the sign bit set
+
+
+def dump_inputs():
+    """The arrays whose dumps are pinned: a 16x8-quad terrain's reference
+    LBVH (2F4 nodes) and Morton-ordered triangles, a 16x4 ray image of the
+    terrain camera, and records of special values appended to each."""
+    from oracle import oracle as O
+    tris = S.terrain(16, 8, seed=3)
+    lb = O.lbvh_build(tris, 30)
+    nodes = np.asarray(lb.nodes, np.float32).reshape(-1, 8).copy()
+    srt = np.asarray(O.permute(tris, lb.ids), np.float32).reshape(-1, 26).copy()
+    sp = SPECIALS
+    extra_nodes = np.zeros((4, 8), np.float32)
+    words = np.array([[(7 << 1) | 1, 9], [3 << 1, 250], [0, 0], [(1 << 24) << 1 | 1, 4000000000]], np.uint32)
+    extra_nodes[:, :2] = words.view(np.float32)
+    extra_nodes[:, 2:] = np.resize(sp, (4, 6))
+    extra_tris = np.resize(sp, (3, 26)).astype(np.float32)
+    cam = S.Camera((0.0, 0.6, 1.6), (0.0, 0.0, 0.0), fovy=60.0, w=16, h=4)
+    o, d, m = O.shirley_rays(cam.tan_half, cam.aspect, cam.w, cam.h, cam.dir, cam.pos, cam.up)
+    rays = np.concatenate([np.asarray(o, np.float32).reshape(-1, 3), np.asarray(d, np.float32).reshape(-1, 3),
+                           np.asarray(m, np.float32).reshape(-1, 1)], axis=1)
+    rays[-3:, :] = np.resize(sp, (3, 7))
+    return np.concatenate([nodes, extra_nodes]), np.concatenate([srt, extra_tris]), rays, cam.w, cam.h
+
+
+def ref_dumps(tmp, nodes, tris, rays, w, h):
+    np.ascontiguousarray(nodes, np.float32).tofile(os.path.join(tmp, "dn.f32"))
+    np.ascontiguousarray(tris, np.float32).tofile(os.path.join(tmp, "dt.f32"))
+    np.ascontiguousarray(rays, np.float32).tofile(os.path.join(tmp, "dr.f32"))
+    prefix = os.path.join(tmp, "dump")
+    subprocess.run([os.path.join(REFDIR, "dump_harness"), os.path.join(tmp, "dn.f32"), str(nodes.shape[0]),
+                    os.path.join(tmp, "dt.f32"), str(tris.shape[0]), os.path.join(tmp, "dr.f32"), str(w), str(h),
+                    prefix], check=True)
+    out = {}
+    for ext in ("bvh", "tri", "ray"):
+        with open(f"{prefix}.{ext}", "rb") as f:
+            out[ext] = np.frombuffer(f.read(), np.uint8)
+    return out
+
+
+def make_dumps(tmp):
+    nodes, tris, rays, w, h = dump_inputs()
+    txt = ref_dumps(tmp, nodes, tris, rays, w, h)
+    np.savez_compressed(os.path.join(OUT, "mamo_dumps.npz"), nodes=nodes, tris=tris, rays=rays, w=w, h=h,
+                        bvh_text=txt["bvh"], tri_text=txt["tri"], ray_text=txt["ray"])
+
+
 def main():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "refbuild"), f"REF={REF}"],
                    check=True)
+    if len(sys.argv) > 1 and sys.argv[1] == "dumps":
+        with tempfile.TemporaryDirectory() as tmp:
+            make_dumps(tmp)
+        print("mamo_dumps.npz", os.path.getsize(os.path.join(OUT, "mamo_dumps.npz")))
+        return
     with tempfile.TemporaryDirectory() as tmp:
         out = {}
         for name, pos in small_cases().items():
@@ -192,7 +255,8 @@ def main():
         for mode in ("cis", "dis"):
             tt[f"{mode}_hits"] = ref_trace(tmp, mode, lb, rays)
         np.savez_compressed(os.path.join(OUT, "terrain_trace.npz"), **tt)
-    for f in ("lbvh_cases.npz", "sphere_trace.npz", "terrain_trace.npz", "shade_sphere.npz"):
+        make_dumps(tmp)
+    for f in ("lbvh_cases.npz", "sphere_trace.npz", "terrain_trace.npz", "shade_sphere.npz", "mamo_dumps.npz"):
         print(f, os.path.getsize(os.path.join(OUT, f)))
 
 

@@ -42,7 +42,7 @@ def test_tune_cache_rejects_bad_keys_and_parameters(tmp_path, lib):
     ok = L.BatchParams(8, 12, 0, 40)
     assert lib.rta_tune_cache_store(path, b'bad"key', C.byref(ok), 1.0) == L.ERR_INVALID
     assert lib.rta_tune_cache_store(path, b"", C.byref(ok), 1.0) == L.ERR_INVALID
-    for bad in (L.BatchParams(9, 12, 0, 40), L.BatchParams(8, 0, 0, 40), L.BatchParams(8, 33, 0, 40),
+    for bad in (L.BatchParams(12, 12, 0, 40), L.BatchParams(8, 0, 0, 40), L.BatchParams(8, 33, 0, 40),
                 L.BatchParams(8, 12, -1, 40), L.BatchParams(8, 12, 0, 48)):
         assert lib.rta_tune_cache_store(path, b"k", C.byref(bad), 1.0) == L.ERR_INVALID
 

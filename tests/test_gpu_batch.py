@@ -161,7 +161,7 @@ def test_autotune_picks_valid_parameters_and_caches_them(work, tmp_path):
     hits = torch.zeros(4 * work.n_rays, dtype=torch.float32, device="cuda")
     chosen, ms = b.autotune(work.tris, work.orig, work.dirs, work.maxt, hits, cache_path=cache, reps=2)
     assert ms > 0
-    assert chosen["digit_bits"] in (8, 10, 11) and chosen["stack"] in (40, 64)
+    assert chosen["digit_bits"] in (8, 9, 10, 11) and chosen["stack"] in (40, 64)
     assert b.params == chosen
     with open(cache) as f:
         entries = json.load(f)
@@ -179,7 +179,7 @@ def test_autotune_picks_valid_parameters_and_caches_them(work, tmp_path):
     assert os.path.getsize(cache) > 0
 
 
-@pytest.mark.parametrize("digit_bits", [8, 10, 11])
+@pytest.mark.parametrize("digit_bits", [8, 9, 10, 11])
 def test_one_mesh_builds_after_batch_builds(work, digit_bits):
     """A batch build and a one-mesh build of the same key width instantiate
     the same sort kernel in two translation units; each must launch its own

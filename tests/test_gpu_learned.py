@@ -126,3 +126,55 @@ def test_learned_order_keeps_closest_hits(case, terrain_case, cluster_case):
     ties = hit & (a["ref"] != b["ref"])
     assert ties.mean() < 1e-3   # ties and those ulp cases may report another triangle
     assert bvh.status() & 0x3F & ~0xC == 0
+
+
+def _plain_rule_params(model):
+    """Weights whose logit is feature 13, the plain rule's choice (+1 left
+    first, -1 right first): h1 = relu(+-x13), h2 = h1, logit = h2[0] - h2[1]."""
+    p = np.zeros_like(model.params())
+    hid, inp = 32, 16
+    w1 = p[: hid * inp].reshape(hid, inp)
+    w1[0, 13], w1[1, 13] = 1.0, -1.0
+    off_w2 = hid * inp + hid
+    w2 = p[off_w2: off_w2 + hid * hid].reshape(hid, hid)
+    w2[0, 0] = w2[1, 1] = 1.0
+    off_w3 = off_w2 + hid * hid + hid
+    p[off_w3 + 0], p[off_w3 + 1] = 1.0, -1.0
+    return p
+
+
+@pytest.mark.parametrize("case", ["terrain", "clusters"])
+def test_inference_reproduces_a_known_rule(case, terrain_case, cluster_case):
+    """With weights that output the plain rule's own choice, the fused
+    tensor-core inference must pick exactly the plain order at every
+    decision: every hit and every ray's node and triangle counts equal those
+    of the plain traversal.  A huge margin (the network never overrides)
+    gives the plain traversal for any weights."""
+    if case == "terrain":
+        _, bvh, g = terrain_case
+        o, d, m = g.gpu_origin, g.gpu_direction, g.gpu_maxt
+    else:
+        _, bvh, (o, d, m) = cluster_case
+    want, sp = LR.plain_trace(bvh, o, d, m, stats=True)
+    model = LR.OrderModel(max_samples=1 << 10, seed=2)
+    model.set_params(_plain_rule_params(model))
+    assert model.margin() == 0.0
+    got, st = model.trace(bvh, o, d, m, stats=True)
+    torch.cuda.synchronize()
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), want.cpu().numpy().view(np.uint32))
+    np.testing.assert_array_equal(st.cpu().numpy(), sp.cpu().numpy())
+    # the opposite rule (logit = -x13) visits more nodes with the same hits
+    anti_p = _plain_rule_params(model)
+    off_w3 = 32 * 16 + 32 + 32 * 32 + 32
+    anti_p[off_w3], anti_p[off_w3 + 1] = -1.0, 1.0
+    model.set_params(anti_p)
+    anti, sa = model.trace(bvh, o, d, m, stats=True)
+    assert int(sa.sum()) > int(sp.sum())
+    hit = hits_np(want)["t"] != np.float32(S.FLT_MAX)
+    np.testing.assert_array_equal(hits_np(anti)["t"] != np.float32(S.FLT_MAX), hit)
+    # random weights under a margin no logit reaches: the plain traversal again
+    model2 = LR.OrderModel(max_samples=1 << 10, seed=9)
+    model2.set_margin(3.0e38)
+    got2, st2 = model2.trace(bvh, o, d, m, stats=True)
+    assert np.array_equal(got2.cpu().numpy().view(np.uint32), want.cpu().numpy().view(np.uint32))
+    np.testing.assert_array_equal(st2.cpu().numpy(), sp.cpu().numpy())

@@ -136,7 +136,7 @@ def test_build_signed_zero_ties_match_the_oracle(bits):
     assert_build_equals(bvh, codes, lb.ids, lb.nodes)
 
 
-@pytest.mark.parametrize("digit_bits", [10, 11])
+@pytest.mark.parametrize("digit_bits", [9, 10, 11])
 @pytest.mark.parametrize("bits", [30, 63])
 def test_sort_digit_width_gives_the_same_tree(digit_bits, bits):
     """The stable LSD sort gives one order whatever its digit width (an odd
