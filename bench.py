@@ -351,6 +351,13 @@ def learned_eval(args, dev):
         tl = timed(lambda: L.check(lib.rta_trace_learned(C.byref(bvh.view), model.handle, P._ptr(o), P._ptr(d),
                                                          P._ptr(m), nr, None, P._ptr(hbuf), None, P._stream()),
                                    "trace_learned"))
+        # the cost of asking the network at every overlapping decision (margin 0)
+        kept_margin = model.margin()
+        model.set_margin(0.0)
+        tn = timed(lambda: L.check(lib.rta_trace_learned(C.byref(bvh.view), model.handle, P._ptr(o), P._ptr(d),
+                                                         P._ptr(m), nr, None, P._ptr(hbuf), None, P._stream()),
+                                   "trace_learned"))
+        model.set_margin(kept_margin)
         work_p, work_l = float(spn.sum()), float(sln.sum())
         out[fam] = {
             "train_samples": samples, "train_loss_before": loss0, "train_loss_after": loss,
@@ -362,7 +369,8 @@ def learned_eval(args, dev):
             "plain": {"nodes_per_ray": float(spn[0]), "tris_per_ray": float(spn[1]), "ms": tp,
                       "mrays_s": nr / (tp * 1e-3) / 1e6},
             "learned": {"nodes_per_ray": float(sln[0]), "tris_per_ray": float(sln[1]), "ms": tl,
-                        "mrays_s": nr / (tl * 1e-3) / 1e6},
+                        "mrays_s": nr / (tl * 1e-3) / 1e6,
+                        "network_every_decision_mrays_s": nr / (tn * 1e-3) / 1e6},
             "ideal_order": {"nodes_per_ray": float(sin[0]), "tris_per_ray": float(sin[1]),
                             "work_reduction": 1.0 - float(sin.sum()) / work_p},
             "work_reduction": 1.0 - work_l / work_p,

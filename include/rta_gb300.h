@@ -282,8 +282,9 @@ uint32_t rta_order_param_count(void);
 int rta_order_get_params(const rta_order_model *model, float *host_params);
 int rta_order_set_params(rta_order_model *model, const float *host_params);
 /* Confidence margin of rta_trace_learned (default 0): the network's choice is
- * taken only where |logit| > margin, the plain nearer-first order elsewhere;
- * FLT_MAX (or any margin no logit exceeds) gives the plain traversal. */
+ * taken only where |logit| > margin, the plain nearer-first order elsewhere.
+ * A margin of FLT_MAX or more gives the plain traversal, and rta_trace_learned
+ * then runs the plain child-is kernel without evaluating the network. */
 int rta_order_set_margin(rta_order_model *model, float margin);
 int rta_order_get_margin(const rta_order_model *model, float *margin);
 

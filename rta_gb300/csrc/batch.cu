@@ -149,16 +149,14 @@ k_batch_morton(const float *__restrict__ cent, uint32_t n, const uint32_t *__res
 // every inner node of every mesh; Morton-ordered triangles; ids made local
 __global__ void __launch_bounds__(256)
 k_batch_karras(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ codes, uint32_t n,
-               const MeshRec *__restrict__ meshes, NodeRec *__restrict__ nodes, uint32_t *__restrict__ parents,
-               uint32_t *__restrict__ counters)
+               const MeshRec *__restrict__ meshes, uint4 *__restrict__ links, uint32_t *__restrict__ parents)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const MeshRec mr = meshes[(uint32_t)(keys[i] >> 30)];
     const uint32_t li = i - mr.tri_off;
     if (li + 1 < mr.n_tris)
-        karras_node(codes + mr.tri_off, mr.n_tris, li, nodes + mr.node_off, parents + mr.parent_off,
-                    counters + mr.node_off);
+        karras_node(codes + mr.tri_off, mr.n_tris, li, links + mr.node_off, parents + mr.parent_off);
     // the Morton-ordered triangles and mesh-local ids are the refit's (k_refit_seg)
 }
 
@@ -212,6 +210,7 @@ struct rta_batch {
     NodeRec *nodes = nullptr;
     RootRec *roots = nullptr;
     uint32_t *parents = nullptr, *counters = nullptr;   // counters: the refit's crossing-node list
+    uint4 *links = nullptr;                              // Karras links per inner node, read by the refit
     TriRec *tris = nullptr;
     uint32_t *status = nullptr;         // [0] flags, [4] trace queue
     float *rbox = nullptr;              // refit tables (refit_layout)
@@ -231,7 +230,7 @@ static void free_batch(rta_batch *b)
 {
     void *ptrs[] = {b->meshes_d, b->tri_off_d, b->ray_off_d, b->box, b->cent, b->keys0, b->keys1,
                     b->vals0, b->vals1, b->codes, b->scratch, b->nodes, b->roots, b->parents,
-                    b->counters, b->tris, b->status, b->rbox};
+                    b->counters, b->tris, b->status, b->rbox, b->links};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -296,11 +295,11 @@ static int batch_build_impl(rta_batch *b, const void *tris, cudaStream_t s)
     if (rc) return rc;
     b->keys_sorted = ks;
     b->index = vs;
-    k_batch_karras<<<eb, 256, 0, s>>>(ks, b->codes, n, b->meshes_d, b->nodes, b->parents, b->counters);
+    k_batch_karras<<<eb, 256, 0, s>>>(ks, b->codes, n, b->meshes_d, b->links, b->parents);
     if ((rc = check_launch("k_batch_karras"))) return rc;
     const uint32_t inner = n - b->meshes;
-    rc = refit_launch<uint32_t, true>(b->codes, n, b->meshes_d, ks, tin, vs, b->nodes, b->parents, b->tris, b->roots,
-                                      b->rbox, b->counters, inner ? inner : 1u, &hdr->n_cross, &hdr->refit_ticket,
+    rc = refit_launch<uint32_t, true>(b->codes, n, b->meshes_d, ks, tin, vs, b->nodes, b->links, b->parents, b->tris,
+                                      b->roots, b->rbox, b->counters, inner ? inner : 1u, &hdr->n_cross, &hdr->refit_ticket,
                                       b->status, batch_sms(), s);
     if (rc) return rc;
     b->built = true;
@@ -417,6 +416,7 @@ int rta_batch_set_meshes(rta_batch *b, uint32_t meshes, const uint32_t *tri_offs
     RTA_CUDA_TRY(cudaMalloc(&b->roots, (size_t)meshes * sizeof(RootRec)));
     RTA_CUDA_TRY(cudaMalloc(&b->parents, (2 * (size_t)nn - meshes) * 4));
     RTA_CUDA_TRY(cudaMalloc(&b->counters, (inner ? inner : 1) * 4));
+    RTA_CUDA_TRY(cudaMalloc(&b->links, (inner ? inner : 1) * sizeof(uint4)));
     RTA_CUDA_TRY(cudaMalloc(&b->rbox, refit_layout(nn).total * 6 * sizeof(float)));
     RTA_CUDA_TRY(cudaMalloc(&b->tris, (size_t)nn * sizeof(TriRec)));
     RTA_CUDA_TRY(cudaMalloc(&b->status, 64));

@@ -192,13 +192,13 @@ k_morton(const float *__restrict__ cent, uint32_t n, Key *__restrict__ keys,
 template <typename Key>
 __global__ void __launch_bounds__(256)
 k_karras(const Key *__restrict__ codes, const uint32_t *__restrict__ ids, uint32_t n,
-         NodeRec *__restrict__ nodes, uint32_t *__restrict__ parents, uint32_t *__restrict__ counters,
+         uint4 *__restrict__ links, uint32_t *__restrict__ parents,
          const float *__restrict__ tris_in, float *__restrict__ tris_out)
 {
     pdl_enter();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (i + 1 < n) karras_node(codes, n, i, nodes, parents, counters);
+    if (i + 1 < n) karras_node(codes, n, i, links, parents);
     // invert_triangle_permutation_cuda (:557-578): the 104-byte records in
     // Morton order, when asked for (the 48-byte TriRecs are k_refit_seg's)
     if (tris_out) {
@@ -289,6 +289,7 @@ struct rta_lbvh_ctx {
     RootRec *root = nullptr;
     uint32_t *parents = nullptr;
     uint32_t *counters = nullptr;   // refit: the inner nodes that cross a segment border
+    uint4 *links = nullptr;         // Karras links per inner node, read by the refit
     TriRec *tris = nullptr;
     uint32_t *status = nullptr;
     float *rbox = nullptr;   // refit tables: prefix and suffix unions, t1, t2
@@ -330,7 +331,7 @@ static size_t status_words_per_tile(int key_bits)
 static void free_ctx(rta_lbvh_ctx *c)
 {
     void *ptrs[] = {c->keys0, c->keys1, c->vals0, c->vals1, c->cent,    c->partial, c->state, c->scratch,
-                    c->nodes, c->root,  c->parents, c->counters, c->tris, c->status,  c->rbox};
+                    c->nodes, c->root,  c->parents, c->counters, c->tris, c->status,  c->rbox, c->links};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     // the settings and events outlive the buffers
@@ -424,6 +425,7 @@ int rta_lbvh_reserve(rta_lbvh_ctx *c, uint32_t n, int bits)
     RTA_CUDA_TRY(cudaMalloc(&c->root, sizeof(RootRec)));
     RTA_CUDA_TRY(cudaMalloc(&c->parents, (size_t)(2 * n - 1) * 4));
     RTA_CUDA_TRY(cudaMalloc(&c->counters, (size_t)n * 4));
+    RTA_CUDA_TRY(cudaMalloc(&c->links, (size_t)n * sizeof(uint4)));
     RTA_CUDA_TRY(cudaMalloc(&c->tris, (size_t)n * sizeof(TriRec)));
     RTA_CUDA_TRY(cudaMalloc(&c->status, 64));
     RTA_CUDA_TRY(cudaMemset(c->status, 0, 64));
@@ -488,19 +490,19 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
     if (rc) return rc;
     if ((rc = mark(3))) return rc;
     RTA_CUDA_TRY(bits == 63 ? launch_pdl(true, k_karras<uint64_t>, dim3(eb), dim3(256), 0, s,
-                                         (const uint64_t *)c->codes, (const uint32_t *)c->index, n, c->nodes,
-                                         c->parents, c->counters, tin, (float *)tris_out)
+                                         (const uint64_t *)c->codes, (const uint32_t *)c->index, n, c->links,
+                                         c->parents, tin, (float *)tris_out)
                             : launch_pdl(true, k_karras<uint32_t>, dim3(eb), dim3(256), 0, s,
-                                         (const uint32_t *)c->codes, (const uint32_t *)c->index, n, c->nodes,
-                                         c->parents, c->counters, tin, (float *)tris_out));
+                                         (const uint32_t *)c->codes, (const uint32_t *)c->index, n, c->links,
+                                         c->parents, tin, (float *)tris_out));
     if ((rc = mark(4))) return rc;
     const uint32_t cap = n > 1 ? n - 1 : 1;
     rc = bits == 63 ? refit_launch<uint64_t, false>((const uint64_t *)c->codes, n, nullptr, nullptr, tin, c->index,
-                                                    c->nodes, c->parents, c->tris, c->root, c->rbox, c->counters,
+                                                    c->nodes, c->links, c->parents, c->tris, c->root, c->rbox, c->counters,
                                                     cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s,
                                                     true)
                     : refit_launch<uint32_t, false>((const uint32_t *)c->codes, n, nullptr, nullptr, tin, c->index,
-                                                    c->nodes, c->parents, c->tris, c->root, c->rbox, c->counters,
+                                                    c->nodes, c->links, c->parents, c->tris, c->root, c->rbox, c->counters,
                                                     cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s,
                                                     true);
     if (rc) return rc;

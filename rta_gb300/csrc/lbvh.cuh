@@ -222,7 +222,8 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
     // highest lane of a mask is its leader, adds the lane count to the warp's
     // digit counter and clears the word; the others take the old counter
     // from it.  The warp's keys are consecutive in the input (item-major),
-    // so the order is the input order.
+    // so the order is the input order.  (Ranking two items at a time, two
+    // independent chains, measured no faster.)
     const uint32_t lane_bit = 1u << lane;
     const uint32_t le_mask = lane_bit | (lane_bit - 1u);
 #pragma unroll
@@ -237,7 +238,7 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
         uint32_t off = 0;
         if (lane == leader) off = atomicAdd(&S.whist[w][d], upto);   // the leader's upto = all peers
         off = __shfl_sync(0xffffffffu, off, leader);
-        // every lane has read the mask (its value fed the shuffle above)
+        __syncwarp();   // every lane has read the mask
         if (lane == leader) *m = 0u;
         __syncwarp();
         rank[i] = off + upto - 1u;
@@ -407,22 +408,22 @@ __device__ __forceinline__ void karras_split(const Key *__restrict__ codes, int 
     right_size = to - mid;
 }
 
-// links of inner node i (i + 1 < n) of a tree over codes[0, n), its
-// children's parent words, and its refit counter
+// links of inner node i (i + 1 < n) of a tree over codes[0, n) -- (left
+// link, right link, left size, right size), into a compact array the refit
+// reads; the refit writes each node's whole record -- and its children's
+// parent words
 template <typename Key>
 __device__ __forceinline__ void karras_node(const Key *__restrict__ codes, uint32_t n, uint32_t i,
-                                            NodeRec *__restrict__ nodes, uint32_t *__restrict__ parents,
-                                            uint32_t *__restrict__ counters)
+                                            uint4 *__restrict__ links, uint32_t *__restrict__ parents)
 {
     int l, r, ls, rs;
     karras_split(codes, (int)n, (int)i, l, r, ls, rs);
     const uint32_t inner = n - 1;
     uint32_t llink = (uint32_t)l < inner ? (uint32_t)l : make_leaf((uint32_t)l - inner, 1u);
     uint32_t rlink = (uint32_t)r < inner ? (uint32_t)r : make_leaf((uint32_t)r - inner, 1u);
-    nodes[i].q3 = make_uint4(llink, rlink, (uint32_t)ls, (uint32_t)rs);
+    links[i] = make_uint4(llink, rlink, (uint32_t)ls, (uint32_t)rs);
     parents[l] = (i << 1) | 0u;
     parents[r] = (i << 1) | 1u;
-    counters[i] = 0u;
 }
 
 // the Morton-ordered record of one triangle (count 1 until the refit
@@ -459,20 +460,29 @@ __device__ __forceinline__ TriRec make_tri(const float *__restrict__ src, uint32
 // triangle record at l keeps the count of the largest collapsed node that
 // starts there (atomic max; a climb writes the counts bottom-up).
 //
+// Node records are written whole where possible: an inner node whose range
+// lies in one segment takes both children's boxes from the segment's table
+// and writes its 64-byte record (boxes and links, collapsed children as
+// leaf links) in one piece.  Only the children of a node whose range crosses
+// a segment border write their box into its record slot by slot (a few per
+// cent of the nodes); k_refit_ext writes such a node's links.
+//
 // The leaves of all meshes of a batch are one sorted sequence (a mesh's
 // leaves are contiguous), and a node's range never leaves its mesh, so the
 // segment tables below are built across mesh borders and the queries stay
 // exact.  Three launches:
 //   k_refit_seg  one block per 256-leaf segment: a shared-memory sparse table
-//                of the leaf boxes; writes each leaf's box and the box of each
-//                inner node whose range lies in the segment into the parent
-//                record (a mesh's root into its root record), per-leaf prefix
-//                / suffix unions and the segment union, and lists the inner
-//                nodes whose range crosses a segment border;
+//                of the leaf boxes; writes the record of each inner node
+//                whose range lies in the segment (a mesh's root also into its
+//                root record), the box of each leaf and such node whose
+//                parent crosses a border into that parent's record, per-leaf
+//                prefix / suffix unions and the segment union, and lists the
+//                inner nodes whose range crosses a segment border;
 //   k_refit_top  the same tables over the segment unions in 256-entry groups,
 //                and in the last block a full sparse table over the groups;
-//   k_refit_ext  each listed node: suffix of its first segment + segment
-//                unions between + prefix of its last segment.
+//   k_refit_ext  each listed node: its links, and its box = suffix of its
+//                first segment + segment unions between + prefix of its last
+//                segment, into its parent's record (or the root record).
 
 __device__ __forceinline__ void write_slot(NodeRec *nd, uint32_t side, const float lo[3],
                                            const float hi[3])
@@ -617,34 +627,58 @@ __device__ __forceinline__ MeshSpan mesh_of(uint32_t j, uint32_t n_all, const Me
     return MeshSpan{m, mr.tri_off, mr.n_tris, mr.node_off, mr.parent_off};
 }
 
-// inner node c (local to mesh sp) with global range [gl, gr] and box x: into
-// its parent's record, or the mesh's root record for c = 0
-template <typename Key>
-__device__ __forceinline__ void place_node(const Key *__restrict__ codes, const MeshSpan &sp, uint32_t c,
-                                           uint32_t gl, uint32_t gr, const Box6 &x, NodeRec *__restrict__ nodes,
-                                           const uint32_t *__restrict__ parents, TriRec *__restrict__ tris,
-                                           RootRec *__restrict__ roots, uint32_t *__restrict__ flags)
+__device__ __forceinline__ bool crosses_segment(uint32_t gl, uint32_t gr) { return gl / kRefitSeg != gr / kRefitSeg; }
+
+// whether inner node p of mesh sp (local index) has a range that crosses a
+// segment border; false with the bad-link flag for an index out of range
+__device__ __forceinline__ bool node_crosses(const uint4 *__restrict__ links, const MeshSpan &sp, uint32_t p,
+                                             uint32_t *__restrict__ flags)
 {
-    const bool collapsed = codes[gl] == codes[gr];   // a leaf of gr - gl + 1 triangles
-    const uint32_t cnt = gr - gl + 1u;
-    if (collapsed) atomicMax(reinterpret_cast<uint32_t *>(&tris[gl].v0.w), cnt);
-    if (c == 0u) {
-        RootRec &R = roots[sp.m];
-        for (int a = 0; a < 3; ++a) {
-            R.lo[a] = x.lo[a];
-            R.hi[a] = x.hi[a];
-        }
-        R.link = collapsed ? make_leaf(0u, cnt) : 0u;
-        return;
-    }
-    const uint32_t pl = parents[sp.parent_off + c], p = pl >> 1, side = pl & 1u;
-    if (p >= sp.n - 1u) {
+    uint32_t l, r;
+    if (p >= sp.n - 1u || !node_range(links[sp.node_off + p], sp.n, l, r)) {
         atomicOr(flags, RTA_DEV_BAD_LINK);
-        return;
+        return false;
     }
-    NodeRec *nd = nodes + sp.node_off + p;
-    write_slot(nd, side, x.lo, x.hi);
-    if (collapsed) reinterpret_cast<uint32_t *>(&nd->q3)[side] = make_leaf(gl - sp.tri_off, cnt);
+    return crosses_segment(sp.tri_off + l, sp.tri_off + r);
+}
+
+// a child's link in its parent's record: an inner child whose codes are all
+// equal collapses to a leaf of its gr - gl + 1 triangles (the triangle record
+// at gl keeps the largest such count)
+template <typename Key>
+__device__ __forceinline__ uint32_t child_link(const Key *__restrict__ codes, const MeshSpan &sp, uint32_t link,
+                                               uint32_t gl, uint32_t gr, TriRec *__restrict__ tris)
+{
+    if (is_leaf(link) || codes[gl] != codes[gr]) return link;
+    const uint32_t cnt = gr - gl + 1u;
+    atomicMax(reinterpret_cast<uint32_t *>(&tris[gl].v0.w), cnt);
+    return make_leaf(gl - sp.tri_off, cnt);
+}
+
+// a mesh's root record: box, and a leaf link if all its codes are equal
+template <typename Key>
+__device__ __forceinline__ void write_root(const Key *__restrict__ codes, const MeshSpan &sp, const Box6 &x,
+                                           TriRec *__restrict__ tris, RootRec *__restrict__ roots)
+{
+    const uint32_t gl = sp.tri_off, gr = sp.tri_off + sp.n - 1u;
+    const bool collapsed = codes[gl] == codes[gr];
+    if (collapsed) atomicMax(reinterpret_cast<uint32_t *>(&tris[gl].v0.w), sp.n);
+    RootRec &R = roots[sp.m];
+    for (int a = 0; a < 3; ++a) {
+        R.lo[a] = x.lo[a];
+        R.hi[a] = x.hi[a];
+    }
+    R.link = collapsed ? make_leaf(0u, sp.n) : 0u;
+}
+
+// a whole inner-node record: both children's boxes, planes interleaved as
+// (left, right, left, right) per axis, and the links
+__device__ __forceinline__ void write_record(NodeRec *nd, const Box6 &L, const Box6 &R, const uint4 q3)
+{
+    nd->q0 = make_float4(L.lo[0], R.lo[0], L.hi[0], R.hi[0]);
+    nd->q1 = make_float4(L.lo[1], R.lo[1], L.hi[1], R.hi[1]);
+    nd->q2 = make_float4(L.lo[2], R.lo[2], L.hi[2], R.hi[2]);
+    nd->q3 = q3;
 }
 
 namespace {
@@ -653,7 +687,7 @@ template <typename Key, bool BATCH>
 __global__ void __launch_bounds__(kRefitSeg)
 k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__restrict__ meshes,
             const uint64_t *__restrict__ keys, const float *__restrict__ tris_in, uint32_t *__restrict__ ids,
-            NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
+            NodeRec *__restrict__ nodes, const uint4 *__restrict__ links, const uint32_t *__restrict__ parents,
             TriRec *__restrict__ tris, RootRec *__restrict__ roots, float *__restrict__ pre,
             float *__restrict__ suf, float *__restrict__ seg, uint32_t *__restrict__ cross,
             uint32_t *__restrict__ n_cross, uint32_t *__restrict__ flags)
@@ -666,13 +700,16 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
     Box6 b{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     // this thread's loads are issued before the table build and land meanwhile
     MeshSpan sp{0u, 0u, 1u, 0u, 0u};
-    uint32_t leaf_pl = 0u, jl = 0u;
+    uint32_t leaf_pl = 0u, node_pl = 0u, jl = 0u;
     uint4 q3 = make_uint4(0u, 0u, 0u, 0u);
     if (j < n_all) {
         sp = mesh_of<BATCH>(j, n_all, meshes, keys);
         jl = j - sp.tri_off;
         if (sp.n > 1u) leaf_pl = parents[sp.parent_off + sp.n - 1u + jl];
-        if (jl + 1u < sp.n) q3 = nodes[sp.node_off + jl].q3;
+        if (jl + 1u < sp.n) {
+            q3 = links[sp.node_off + jl];
+            if (jl != 0u) node_pl = parents[sp.parent_off + jl];
+        }
         // invert_triangle_permutation_cuda (lbvh-kernels.cu:557-578): the
         // triangle of sorted position j, in Morton order, with its id local
         // to its mesh (collapse counts land in .w after the table build's
@@ -696,24 +733,34 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
                 R.hi[a] = b.hi[a];
             }
             R.link = make_leaf(0u, 1u);
-        } else if ((leaf_pl >> 1) >= sp.n - 1u) {
-            atomicOr(flags, RTA_DEV_BAD_LINK);
-        } else {   // the leaf's box into its parent's record
+        } else if (node_crosses(links, sp, leaf_pl >> 1, flags)) {
+            // the leaf's box into its parent's record (a parent within one
+            // segment writes its record itself)
             write_slot(nodes + sp.node_off + (leaf_pl >> 1), leaf_pl & 1u, b.lo, b.hi);
         }
-        // inner node jl of the mesh (one end of its range): here when the range
-        // lies in this segment, else on the list for k_refit_ext
+        // inner node jl of the mesh (one end of its range): its record here
+        // when the range lies in this segment, else on the list for k_refit_ext
         uint32_t l, r;
         if (jl + 1u < sp.n) {
             if (!node_range(q3, sp.n, l, r)) {
                 atomicOr(flags, RTA_DEV_BAD_LINK);
             } else {
-                const uint32_t gl = sp.tri_off + l, gr = sp.tri_off + r;
-                if (gl / kRefitSeg == gr / kRefitSeg)
-                    place_node(codes, sp, jl, gl, gr, T.query(gl - base, gr - base), nodes, parents, tris, roots,
-                               flags);
-                else
+                const uint32_t gl = sp.tri_off + l, gr = sp.tri_off + r, gm = gl + q3.z;   // gm: right child's first
+                if (!crosses_segment(gl, gr)) {
+                    const Box6 bl = T.query(gl - base, gm - 1u - base), br = T.query(gm - base, gr - base);
+                    uint4 q = q3;
+                    q.x = child_link(codes, sp, q3.x, gl, gm - 1u, tris);
+                    q.y = child_link(codes, sp, q3.y, gm, gr, tris);
+                    write_record(nodes + sp.node_off + jl, bl, br, q);
+                    if (jl == 0u) {
+                        write_root(codes, sp, box_join(bl, br), tris, roots);
+                    } else if (node_crosses(links, sp, node_pl >> 1, flags)) {
+                        const Box6 x = box_join(bl, br);
+                        write_slot(nodes + sp.node_off + (node_pl >> 1), node_pl & 1u, x.lo, x.hi);
+                    }
+                } else {
                     crosses = true;
+                }
             }
         }
     }
@@ -802,7 +849,8 @@ k_refit_top(float *__restrict__ t1, uint32_t nseg, float *__restrict__ t2, uint3
 template <typename Key, bool BATCH>
 __device__ __forceinline__ void refit_cross(const Key *__restrict__ codes, uint32_t n_all, uint32_t j,
                                             const MeshRec *__restrict__ meshes, const uint64_t *__restrict__ keys,
-                                            NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
+                                            NodeRec *__restrict__ nodes, const uint4 *__restrict__ links,
+                                            const uint32_t *__restrict__ parents,
                                             TriRec *__restrict__ tris, RootRec *__restrict__ roots,
                                             const float *__restrict__ pre, const float *__restrict__ suf,
                                             const float *__restrict__ t1, uint32_t nseg, const float *__restrict__ t2,
@@ -812,8 +860,10 @@ __device__ __forceinline__ void refit_cross(const Key *__restrict__ codes, uint3
     const MeshSpan sp = mesh_of<BATCH>(j, n_all, meshes, keys);
     const uint32_t jl = j - sp.tri_off;
     uint32_t l, r;
-    if (jl + 1u >= sp.n || !node_range(nodes[sp.node_off + jl].q3, sp.n, l, r)) return;
-    const uint32_t gl = sp.tri_off + l, gr = sp.tri_off + r;
+    if (jl + 1u >= sp.n) return;
+    const uint4 q3 = links[sp.node_off + jl];
+    if (!node_range(q3, sp.n, l, r)) return;
+    const uint32_t gl = sp.tri_off + l, gr = sp.tri_off + r, gm = gl + q3.z;
     const uint32_t sa = gl / kRefitSeg, sb = gr / kRefitSeg;
     if (sa == sb) return;
     Box6 x = gload(suf, gl);
@@ -834,13 +884,29 @@ __device__ __forceinline__ void refit_cross(const Key *__restrict__ codes, uint3
         }
     }
     x = box_join(x, gload(pre, gr));
-    place_node(codes, sp, jl, gl, gr, x, nodes, parents, tris, roots, flags);
+    // the node's links (its children write their boxes into its record)
+    uint4 q = q3;
+    q.x = child_link(codes, sp, q3.x, gl, gm - 1u, tris);
+    q.y = child_link(codes, sp, q3.y, gm, gr, tris);
+    nodes[sp.node_off + jl].q3 = q;
+    // its box into its parent's record, whose range crosses a border too
+    if (jl == 0u) {
+        write_root(codes, sp, x, tris, roots);
+        return;
+    }
+    const uint32_t pl = parents[sp.parent_off + jl], p = pl >> 1;
+    if (p >= sp.n - 1u) {
+        atomicOr(flags, RTA_DEV_BAD_LINK);
+        return;
+    }
+    write_slot(nodes + sp.node_off + p, pl & 1u, x.lo, x.hi);
 }
 
 template <typename Key, bool BATCH>
 __global__ void __launch_bounds__(256)
 k_refit_ext(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__restrict__ meshes,
-            const uint64_t *__restrict__ keys, NodeRec *__restrict__ nodes, const uint32_t *__restrict__ parents,
+            const uint64_t *__restrict__ keys, NodeRec *__restrict__ nodes, const uint4 *__restrict__ links,
+            const uint32_t *__restrict__ parents,
             TriRec *__restrict__ tris, RootRec *__restrict__ roots, const float *__restrict__ pre,
             const float *__restrict__ suf, const float *__restrict__ t1, uint32_t nseg,
             const float *__restrict__ t2, uint32_t ngrp, const uint32_t *__restrict__ cross,
@@ -849,8 +915,8 @@ k_refit_ext(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
     pdl_enter();
     const uint32_t count = min(*n_cross, cross_cap);
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x)
-        refit_cross<Key, BATCH>(codes, n_all, cross[e], meshes, keys, nodes, parents, tris, roots, pre, suf, t1,
-                                nseg, t2, ngrp, flags);
+        refit_cross<Key, BATCH>(codes, n_all, cross[e], meshes, keys, nodes, links, parents, tris, roots, pre, suf,
+                                t1, nseg, t2, ngrp, flags);
 }
 
 } // namespace
@@ -883,14 +949,14 @@ inline RefitLayout refit_layout(uint32_t n)
 // inner node: cross_cap), *n_cross and *ticket zero on entry.
 template <typename Key, bool BATCH>
 int refit_launch(const Key *codes, uint32_t n_all, const MeshRec *meshes, const uint64_t *keys,
-                 const float *tris_in, uint32_t *ids, NodeRec *nodes, const uint32_t *parents, TriRec *tris,
-                 RootRec *roots, float *rbox, uint32_t *cross, uint32_t cross_cap, uint32_t *n_cross,
+                 const float *tris_in, uint32_t *ids, NodeRec *nodes, const uint4 *links, const uint32_t *parents,
+                 TriRec *tris, RootRec *roots, float *rbox, uint32_t *cross, uint32_t cross_cap, uint32_t *n_cross,
                  uint32_t *ticket, uint32_t *flags, int sms, cudaStream_t s, bool pdl = false)
 {
     const RefitLayout L = refit_layout(n_all);
     float *pre = rbox + 6 * L.pre, *suf = rbox + 6 * L.suf, *t1 = rbox + 6 * L.t1, *t2 = rbox + 6 * L.t2;
     cudaError_t e = launch_pdl(pdl, k_refit_seg<Key, BATCH>, dim3(L.nseg), dim3(kRefitSeg), 0, s, codes, n_all,
-                               meshes, keys, tris_in, ids, nodes, parents, tris, roots, pre, suf, t1, cross,
+                               meshes, keys, tris_in, ids, nodes, links, parents, tris, roots, pre, suf, t1, cross,
                                n_cross, flags);
     if (e == cudaSuccess)
         e = launch_pdl(pdl, k_refit_top, dim3(L.ngrp), dim3(kRefitSeg), 0, s, t1, L.nseg, t2, L.ngrp, L.levels2,
@@ -898,7 +964,7 @@ int refit_launch(const Key *codes, uint32_t n_all, const MeshRec *meshes, const 
     if (e == cudaSuccess && n_all > 2u) {
         const uint32_t want = (n_all + 255u) / 256u, cap = (uint32_t)sms * 4u;
         e = launch_pdl(pdl, k_refit_ext<Key, BATCH>, dim3(want < cap ? want : cap), dim3(256), 0, s, codes, n_all,
-                       meshes, keys, (NodeRec *)nodes, parents, tris, roots, (const float *)pre,
+                       meshes, keys, (NodeRec *)nodes, links, parents, tris, roots, (const float *)pre,
                        (const float *)suf, (const float *)t1, L.nseg, (const float *)t2, L.ngrp,
                        (const uint32_t *)cross, (const uint32_t *)n_cross, cross_cap, flags);
     }

@@ -316,6 +316,8 @@ __global__ void k_adam(float *__restrict__ p, float *__restrict__ m, float *__re
     if (threadIdx.x == 0) out->b3 = p[kOffB3];
 }
 
+int trace_impl(const rta_lbvh *bvh, const float *orig, const float *dir, const float *maxt, uint32_t nrays,
+               const uint32_t *d_nrays, void *hits, uint32_t mode, uint32_t *stats, uint32_t *queue, cudaStream_t s);
 int trace_learn_impl(const rta_lbvh *bvh, const MlpWeights *w, const float *orig, const float *dir,
                      const float *maxt, uint32_t nrays, const uint32_t *d_nrays, void *hits,
                      uint32_t *stats, Sample *samples, uint32_t *sample_count, uint32_t sample_cap,
@@ -582,6 +584,11 @@ int rta_trace_learned(const rta_lbvh *bvh, const rta_order_model *c, const float
                       uint32_t *stats, rta_stream_t stream)
 {
     if (!bvh || !c || !orig || !dir || !maxt || !hits || (!d_nrays && nrays == 0)) return RTA_ERR_INVALID;
+    // A margin no finite logit exceeds: the network never decides, so the
+    // order is the plain one and the plain child-is kernel runs it
+    if (c->margin >= FLT_MAX)
+        return trace_impl(bvh, orig, dir, maxt, nrays, d_nrays, hits, RTA_TRACE_CIS | (stats ? RTA_TRACE_STATS : 0u),
+                          stats, c->counters + 1, (cudaStream_t)stream);
     return trace_learn_impl(bvh, c->weights, orig, dir, maxt, nrays, d_nrays, hits, stats, nullptr, nullptr,
                             0, c->counters + 1, true, (cudaStream_t)stream);
 }

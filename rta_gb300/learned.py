@@ -181,7 +181,8 @@ def choose_margin(model: OrderModel, bvh, orig, dirs, maxt, candidates=MARGINS) 
         table[repr(mg)] = w
         if w < best_w or (w == best_w and mg > best_m):
             best_m, best_w = mg, w
-    model.set_margin(3.0e38 if best_m == float("inf") else best_m)
+    # an infinite choice is FLT_MAX, which runs the plain kernel (no network)
+    model.set_margin(float(np.finfo(np.float32).max) if best_m == float("inf") else best_m)
     return {"margin": best_m, "work_per_ray": best_w, "plain_work_per_ray": plain, "tried": table}
 
 

@@ -172,9 +172,12 @@ def test_inference_reproduces_a_known_rule(case, terrain_case, cluster_case):
     assert int(sa.sum()) > int(sp.sum())
     hit = hits_np(want)["t"] != np.float32(S.FLT_MAX)
     np.testing.assert_array_equal(hits_np(anti)["t"] != np.float32(S.FLT_MAX), hit)
-    # random weights under a margin no logit reaches: the plain traversal again
+    # random weights under a margin no logit reaches: the plain traversal
+    # again, through the network kernel (3e38) and through the plain kernel
+    # that FLT_MAX selects
     model2 = LR.OrderModel(max_samples=1 << 10, seed=9)
-    model2.set_margin(3.0e38)
-    got2, st2 = model2.trace(bvh, o, d, m, stats=True)
-    assert np.array_equal(got2.cpu().numpy().view(np.uint32), want.cpu().numpy().view(np.uint32))
-    np.testing.assert_array_equal(st2.cpu().numpy(), sp.cpu().numpy())
+    for margin in (3.0e38, float(np.finfo(np.float32).max)):
+        model2.set_margin(margin)
+        got2, st2 = model2.trace(bvh, o, d, m, stats=True)
+        assert np.array_equal(got2.cpu().numpy().view(np.uint32), want.cpu().numpy().view(np.uint32))
+        np.testing.assert_array_equal(st2.cpu().numpy(), sp.cpu().numpy())
