@@ -441,7 +441,16 @@ def incoherent_eval(args, dev):
     torch.cuda.synchronize()
     hit_frac = float((hits.view(-1, 4)[:, 0] < 3.0e38).to(torch.float64).mean())
     alg = 504 * n   # build bytes per triangle with 63-bit keys (8 sort passes of 12-byte keys+ids)
-    peak, _ = measured_peaks()
+    peak, peak_src = measured_peaks()
+    # the trace's algorithmic bytes, as for the frame: 28 B ray + 16 B hit per
+    # ray, 64 B per inner node visited (one two-child record), 48 B per
+    # triangle tested
+    trace_alg = nr * (28 + 16) + float(w[0]) * nr * 64 + float(w[1]) * nr * 48
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "trace_traffic_incoherent.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
     return {
         "triangles": n, "morton_bits": 63, "rays": nr, "hit_fraction": hit_frac,
         "build_ms": build_ms, "build_mtri_s": n / (build_ms * 1e-3) / 1e6,
@@ -449,6 +458,12 @@ def incoherent_eval(args, dev):
         "build_frac_of_peak": alg / (build_ms * 1e-3) / 1e9 / peak,
         "trace_ms": trace_ms, "trace_mrays_s": nr / (trace_ms * 1e-3) / 1e6,
         "inner_visits_per_ray": float(w[0]), "tri_tests_per_ray": float(w[1]),
+        "trace_roofline": {
+            "bound": "hbm", "kernel": "k_trace<CIS> over the 63-bit cluster tree (80-entry stack)",
+            "achieved": trace_alg / (trace_ms * 1e-3) / 1e9, "peak": peak, "peak_source": peak_src,
+            "unit": "GB/s", "frac": trace_alg / (trace_ms * 1e-3) / 1e9 / peak,
+            "algorithmic_bytes_per_launch": trace_alg, "traffic": traffic,
+            "note": "latency bound: nodes are fetched from L1/L2; traffic = DRAM bytes of one launch (ncu)"},
     }
 
 

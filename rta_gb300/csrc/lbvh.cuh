@@ -130,7 +130,7 @@ struct SortSmem {
     uint32_t whist[kSortThreads / 32][kRadix];
     uint32_t digit_start[kRadix];
     uint32_t glob[kRadix];
-    uint32_t scan_tmp[kSortThreads / 32];
+    uint32_t scan_tmp[2 * (kSortThreads / 32)];
     uint32_t tile;
     // the ranking's lane masks are dead once the tile is ranked, the staging
     // area is live only afterwards: they share the space
@@ -143,32 +143,48 @@ struct SortSmem {
     } u;
 };
 
-// block-wide exclusive scan of one value per thread (256 threads)
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *tmp)
+// block-wide exclusive scans of two values per thread (256 threads) with
+// one set of barriers; tmp holds 2 words per warp
+__device__ __forceinline__ void block_excl_scan2(uint32_t a, uint32_t b, uint32_t *tmp, uint32_t &ea,
+                                                 uint32_t &eb)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t x = v;
+    uint32_t x = a, y = b;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
-        if (lane >= off) x += y;
+        const uint32_t u = __shfl_up_sync(0xffffffffu, x, off);
+        const uint32_t v = __shfl_up_sync(0xffffffffu, y, off);
+        if (lane >= off) {
+            x += u;
+            y += v;
+        }
     }
-    if (lane == 31) tmp[w] = x;
+    if (lane == 31) {
+        tmp[2 * w] = x;
+        tmp[2 * w + 1] = y;
+    }
     __syncthreads();
     if (w == 0) {
-        uint32_t t = lane < kSortThreads / 32 ? tmp[lane] : 0u;
+        uint32_t p = lane < kSortThreads / 32 ? tmp[2 * lane] : 0u;
+        uint32_t q = lane < kSortThreads / 32 ? tmp[2 * lane + 1] : 0u;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, t, off);
-            if (lane >= off) t += y;
+            const uint32_t u = __shfl_up_sync(0xffffffffu, p, off);
+            const uint32_t v = __shfl_up_sync(0xffffffffu, q, off);
+            if (lane >= off) {
+                p += u;
+                q += v;
+            }
         }
-        if (lane < kSortThreads / 32) tmp[lane] = t;
+        if (lane < kSortThreads / 32) {
+            tmp[2 * lane] = p;
+            tmp[2 * lane + 1] = q;
+        }
     }
     __syncthreads();
-    uint32_t before = w ? tmp[w - 1] : 0u;
-    uint32_t r = before + x - v;
+    ea = (w ? tmp[2 * (w - 1)] : 0u) + x - a;
+    eb = (w ? tmp[2 * (w - 1) + 1] : 0u) + y - b;
     __syncthreads();
-    return r;
 }
 
 // The kernel and its launcher have internal linkage: build.cu and batch.cu
@@ -206,6 +222,11 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
     const uint32_t tile = S.tile;
     const uint32_t base = tile * kSortTile;
     const uint32_t wbase = base + (uint32_t)w * (32 * kSortItems);
+
+    // this pass's global digit counts, loaded now and used after the ranking
+    uint32_t gh[kDpt];
+#pragma unroll
+    for (int j = 0; j < kDpt; ++j) gh[j] = tid * kDpt + j < kRadix ? hist[tid * kDpt + j] : 0u;
 
     Key k[kSortItems];
     uint32_t v[kSortItems];
@@ -247,7 +268,7 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
 
     // per digit (thread tid owns digits tid*kDpt .. tid*kDpt+kDpt-1): warp
     // offsets, tile count, block offsets
-    uint32_t cnt[kDpt], gh[kDpt];
+    uint32_t cnt[kDpt];
     uint32_t csum = 0, gsum = 0;
     // padding keys (beyond n) are all the last digit and sit at the end of the last tile
     const uint32_t valid = n - base < (uint32_t)kSortTile ? n - base : (uint32_t)kSortTile;
@@ -256,7 +277,6 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
     for (int j = 0; j < kDpt; ++j) {
         const int d = tid * kDpt + j;
         cnt[j] = 0;
-        gh[j] = 0;
         if (d < kRadix) {
 #pragma unroll
             for (int q = 0; q < kSortThreads / 32; ++q) {
@@ -264,7 +284,6 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
                 S.whist[q][d] = cnt[j];
                 cnt[j] += c;
             }
-            gh[j] = hist[d];
             const uint32_t cv = (d == kRadix - 1) ? cnt[j] - pad : cnt[j];
             uint32_t *my_stat = tstat + (size_t)tile * kRadix + d;
             st_volatile(my_stat, (tile == 0 ? kStatPrefix : kStatAggregate) | cv);
@@ -272,33 +291,49 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
         csum += cnt[j];
         gsum += gh[j];
     }
-    uint32_t start = block_excl_scan(csum, S.scan_tmp);
-    uint32_t gexcl = block_excl_scan(gsum, S.scan_tmp);
+    uint32_t start0, gexcl0;
+    block_excl_scan2(csum, gsum, S.scan_tmp, start0, gexcl0);
+    uint32_t dstart[kDpt];
+    {
+        uint32_t start = start0;
 #pragma unroll
-    for (int j = 0; j < kDpt; ++j) {
-        const int d = tid * kDpt + j;
-        if (d < kRadix) {
-            const uint32_t cv = (d == kRadix - 1) ? cnt[j] - pad : cnt[j];
-            uint32_t excl = 0;
-            if (tile > 0) {
-                excl = lookback(tstat + d, kRadix, tile, flags);
-                __threadfence();
-                st_volatile(tstat + (size_t)tile * kRadix + d, kStatPrefix | ((excl + cv) & kStatValue));
-            }
-            S.digit_start[d] = start;
-            S.glob[d] = gexcl + excl - start;
+        for (int j = 0; j < kDpt; ++j) {
+            const int d = tid * kDpt + j;
+            dstart[j] = start;
+            if (d < kRadix) S.digit_start[d] = start;
+            start += cnt[j];
         }
-        start += cnt[j];
-        gexcl += gh[j];
     }
     __syncthreads();
 
+    // the tile in digit order in shared memory; meanwhile the predecessor
+    // tiles get further with their prefixes
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
         const uint32_t d = (uint32_t)(k[i] >> shift) & kDigitMask;
         uint32_t pos = S.digit_start[d] + S.whist[w][d] + rank[i];
         S.u.stage.keys[pos] = k[i];
         S.u.stage.vals[pos] = v[i];
+    }
+    {
+        uint32_t gexcl = gexcl0;
+#pragma unroll
+        for (int j = 0; j < kDpt; ++j) {
+            const int d = tid * kDpt + j;
+            if (d < kRadix) {
+                const uint32_t cv = (d == kRadix - 1) ? cnt[j] - pad : cnt[j];
+                uint32_t excl = 0;
+                if (tile > 0) {
+                    // a status word carries its flag and its count in one
+                    // 32-bit store and nothing else is read on its account,
+                    // so no fence orders it against other memory
+                    excl = lookback(tstat + d, kRadix, tile, flags);
+                    st_volatile(tstat + (size_t)tile * kRadix + d, kStatPrefix | ((excl + cv) & kStatValue));
+                }
+                S.glob[d] = gexcl + excl - dstart[j];
+            }
+            gexcl += gh[j];
+        }
     }
     __syncthreads();
     for (uint32_t j = tid; j < valid; j += kSortThreads) {
