@@ -172,6 +172,8 @@ k_morton(const float *__restrict__ cent, uint32_t n, Key *__restrict__ keys,
     const float lo[3] = {st->lo[0], st->lo[1], st->lo[2]};
     const float d[3] = {st->scale[0], st->scale[1], st->scale[2]};
     bool wrapped = false;
+    // (one atomic per run of equal digits in a warp, found by shuffles and
+    // ballots, measured slower: 4M 63-bit 36.5 -> 65.5 us)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float c[3] = {cent[(size_t)i * 3 + 0], cent[(size_t)i * 3 + 1], cent[(size_t)i * 3 + 2]};
         Key k = (Key)morton_code(c, lo, d, grid_mask, wrapped);
