@@ -415,13 +415,15 @@ template <> struct KeyBits<uint64_t> {
 };
 
 // common prefix length with the index tie-break (`__cpl`, :84-92)
+// (clz of a zero key difference is the key width, which is the tie-break's
+// base, so equal codes need no branch)
 template <typename Key>
 __device__ __forceinline__ int cpl(const Key *__restrict__ codes, int n, int i, int j, Key ki)
 {
-    if (j < 0 || j >= n) return -1;
-    Key kj = __ldg(codes + j);
-    if (ki == kj) return KeyBits<Key>::tie + __clz(i ^ j);
-    return KeyBits<Key>::clz(ki ^ kj);
+    if ((unsigned)j >= (unsigned)n) return -1;
+    const Key x = ki ^ __ldg(codes + j);
+    const int c = KeyBits<Key>::clz(x);
+    return x == 0 ? c + __clz(i ^ j) : c;
 }
 
 template <typename Key>

@@ -149,6 +149,41 @@ def test_sort_digit_width_gives_the_same_tree(digit_bits, bits):
     assert_build_equals(bvh, codes, lb.ids, lb.nodes)
 
 
+def _skewed_scene(kind, n, seed):
+    """Triangle sets whose sort digits are badly skewed: `clump` puts all but
+    every 997th triangle on one centroid (almost every key equal, so every
+    pass sends nearly a whole tile to one digit), `two` splits them between
+    two tiny far-apart clumps (two digits per pass), `ramp` repeats each of
+    a few hundred positions in runs that straddle the 4096-key tiles."""
+    rng = np.random.default_rng(seed)
+    if kind == "clump":
+        pos = np.tile(rng.uniform(-1, 1, 9), (n, 1))
+        pos[::997] = rng.uniform(-1, 1, (len(pos[::997]), 9))
+    elif kind == "two":
+        a, b = rng.uniform(-1, 1, 9), rng.uniform(-1, 1, 9) + 50.0
+        pos = np.where((np.arange(n) % 3 == 0)[:, None], a, b) + rng.normal(0, 1e-6, (n, 9))
+    else:
+        base = rng.uniform(-1, 1, (331, 9))
+        pos = base[(np.arange(n) // 1500) % 331]
+    return records(pos.astype(np.float32))
+
+
+@pytest.mark.parametrize("kind", ["clump", "two", "ramp"])
+@pytest.mark.parametrize("digit_bits", [8, 11])
+@pytest.mark.parametrize("bits", [30, 63])
+def test_sort_skewed_digits_give_the_oracle_tree(kind, digit_bits, bits):
+    """The onesweep ranking, look-back and scatter under heavy digit skew
+    (lane masks of whole warps on one digit, runs of equal keys across tile
+    borders, a partial last tile): codes, ids and every node word equal the
+    oracle's stable sort and tree."""
+    tris = _skewed_scene(kind, 100_003, seed={"clump": 1, "two": 2, "ramp": 3}[kind])
+    lb = O.lbvh_build(tris, bits)
+    ctor = P.lbvh_constructor(morton_bits=bits, digit_bits=digit_bits)
+    bvh = ctor.build(P.cuda_ftl(tris))
+    codes = lb.codes if bits == 63 else lb.codes.astype(np.uint32)
+    assert_build_equals(bvh, codes, lb.ids, lb.nodes)
+
+
 def test_rebuild_reuses_buffers_and_matches():
     """Rebuilding with a second, smaller scene through the same constructor
     (the -R path, rta/main.cpp:389-400) gives that scene's tree."""
