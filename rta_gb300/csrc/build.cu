@@ -191,33 +191,16 @@ k_morton(const float *__restrict__ cent, uint32_t n, Key *__restrict__ keys,
 // kernel: Karras radix tree + Morton-ordered triangles                        //
 // ------------------------------------------------------------------------- //
 
-// Inner nodes whose range is longer than this go to k_karras_long.
-#ifndef RTA_KARRAS_DEFER_LEN
-#define RTA_KARRAS_DEFER_LEN 64
-#endif
-
 template <typename Key>
 __global__ void __launch_bounds__(256)
 k_karras(const Key *__restrict__ codes, const uint32_t *__restrict__ ids, uint32_t n,
          uint4 *__restrict__ links, uint32_t *__restrict__ parents,
-         const float *__restrict__ tris_in, float *__restrict__ tris_out, uint32_t *__restrict__ deferred,
-         uint32_t *__restrict__ n_deferred)
+         const float *__restrict__ tris_in, float *__restrict__ tris_out)
 {
     pdl_enter();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const bool defer = i + 1 < n && !karras_node(codes, n, i, links, parents, RTA_KARRAS_DEFER_LEN);
-    // the warp's lanes with i < n (a prefix of the warp) list their deferred nodes
-    const uint32_t lane = threadIdx.x & 31u, first = i - lane;
-    const uint32_t live = n - first >= 32u ? 0xffffffffu : (1u << (n - first)) - 1u;
-    const uint32_t dm = __ballot_sync(live, defer);
-    if (dm) {
-        const int leader = __ffs(dm) - 1;
-        uint32_t at = 0;
-        if ((int)lane == leader) at = atomicAdd(n_deferred, (uint32_t)__popc(dm));
-        at = __shfl_sync(live, at, leader);
-        if (defer) deferred[at + __popc(dm & ((1u << lane) - 1u))] = i;
-    }
+    if (i + 1 < n) karras_node(codes, n, i, links, parents);
     // invert_triangle_permutation_cuda (:557-578): the 104-byte records in
     // Morton order, when asked for (the 48-byte TriRecs are k_refit_seg's)
     if (tris_out) {
@@ -228,18 +211,6 @@ k_karras(const Key *__restrict__ codes, const uint32_t *__restrict__ ids, uint32
 #pragma unroll
         for (int j = 0; j < kTriFloats / 2; ++j) d2[j] = __ldg(s2 + j);
     }
-}
-
-// the deferred inner nodes of k_karras: whole warps of long range searches
-template <typename Key>
-__global__ void __launch_bounds__(256)
-k_karras_long(const Key *__restrict__ codes, uint32_t n, uint4 *__restrict__ links, uint32_t *__restrict__ parents,
-              const uint32_t *__restrict__ deferred, const uint32_t *__restrict__ n_deferred)
-{
-    pdl_enter();
-    const uint32_t count = min(*n_deferred, n);
-    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x)
-        karras_node(codes, n, deferred[e], links, parents);
 }
 
 // ------------------------------------------------------------------------- //
@@ -523,23 +494,12 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
                     : sort_keys<uint32_t>(c, n, passes, hdr, tstat, s);
     if (rc) return rc;
     if ((rc = mark(3))) return rc;
-    // the refit's crossing-node list is free until the refit: it holds the
-    // deferred Karras nodes meanwhile
     RTA_CUDA_TRY(bits == 63 ? launch_pdl(true, k_karras<uint64_t>, dim3(eb), dim3(256), 0, s,
                                          (const uint64_t *)c->codes, (const uint32_t *)c->index, n, c->links,
-                                         c->parents, tin, (float *)tris_out, c->counters, &hdr->n_deferred)
+                                         c->parents, tin, (float *)tris_out)
                             : launch_pdl(true, k_karras<uint32_t>, dim3(eb), dim3(256), 0, s,
                                          (const uint32_t *)c->codes, (const uint32_t *)c->index, n, c->links,
-                                         c->parents, tin, (float *)tris_out, c->counters, &hdr->n_deferred));
-    {
-        const int kb = num_sms() * 4;
-        RTA_CUDA_TRY(bits == 63 ? launch_pdl(true, k_karras_long<uint64_t>, dim3(kb), dim3(256), 0, s,
-                                             (const uint64_t *)c->codes, n, c->links, c->parents,
-                                             (const uint32_t *)c->counters, (const uint32_t *)&hdr->n_deferred)
-                                : launch_pdl(true, k_karras_long<uint32_t>, dim3(kb), dim3(256), 0, s,
-                                             (const uint32_t *)c->codes, n, c->links, c->parents,
-                                             (const uint32_t *)c->counters, (const uint32_t *)&hdr->n_deferred));
-    }
+                                         c->parents, tin, (float *)tris_out));
     if ((rc = mark(4))) return rc;
     const uint32_t cap = n > 1 ? n - 1 : 1;
     rc = bits == 63 ? refit_launch<uint64_t, false>((const uint64_t *)c->codes, n, nullptr, nullptr, tin, c->index,

@@ -46,7 +46,6 @@ struct SortScratchHeader {
     uint32_t hist[kMaxPasses * kMaxRadix];
     uint32_t n_cross;        // refit: inner nodes whose range crosses a segment border
     uint32_t refit_ticket;   // refit: last-group ticket of the group tables
-    uint32_t n_deferred;     // Karras: nodes whose range search was left to the second launch
 };
 
 // radix passes for `key_bits` bits at `digit_bits` per pass
@@ -427,13 +426,12 @@ __device__ __forceinline__ int cpl(const Key *__restrict__ codes, int n, int i, 
     return x == 0 ? c + __clz(i ^ j) : c;
 }
 
-// Returns false, having written nothing, when the range end search passes
-// max_len: the caller defers such a node to a second launch whose warps all
-// hold long searches (the trip counts of one warp's searches then stay
-// alike instead of waiting on its one long-range node).
+// (Leaving the nodes whose range search passes 64 leaves to a second launch,
+// so that one warp's searches have alike trip counts, measured no faster:
+// the serialised passes went 29 -> 41 us at 1M and 105 -> 112 us at 4M.)
 template <typename Key>
-__device__ __forceinline__ bool karras_split(const Key *__restrict__ codes, int n, int i, int &left,
-                                             int &right, int &left_size, int &right_size, int max_len)
+__device__ __forceinline__ void karras_split(const Key *__restrict__ codes, int n, int i, int &left,
+                                             int &right, int &left_size, int &right_size)
 {
     // build_tree_karras (:205-249): direction, range end (exponential +
     // binary search), split (binary search with ceiling halving)
@@ -442,10 +440,7 @@ __device__ __forceinline__ bool karras_split(const Key *__restrict__ codes, int 
     int d = dd >= 0 ? 1 : -1;
     int cpl_min = cpl(codes, n, i, i - d, ki);
     int l_max = 2;
-    while (cpl(codes, n, i, i + l_max * d, ki) > cpl_min) {
-        l_max *= 2;
-        if (l_max > max_len) return false;
-    }
+    while (cpl(codes, n, i, i + l_max * d, ki) > cpl_min) l_max *= 2;
     int l = 0;
     for (int t = l_max / 2; t >= 1; t /= 2)
         if (cpl(codes, n, i, i + (l + t) * d, ki) > cpl_min) l += t;
@@ -463,7 +458,6 @@ __device__ __forceinline__ bool karras_split(const Key *__restrict__ codes, int 
     right = (to == mid + 1) ? mid + 1 + n - 1 : mid + 1;
     left_size = mid - from + 1;
     right_size = to - mid;
-    return true;
 }
 
 // links of inner node i (i + 1 < n) of a tree over codes[0, n) -- (left
@@ -471,19 +465,17 @@ __device__ __forceinline__ bool karras_split(const Key *__restrict__ codes, int 
 // reads; the refit writes each node's whole record -- and its children's
 // parent words
 template <typename Key>
-__device__ __forceinline__ bool karras_node(const Key *__restrict__ codes, uint32_t n, uint32_t i,
-                                            uint4 *__restrict__ links, uint32_t *__restrict__ parents,
-                                            int max_len = 0x7fffffff)
+__device__ __forceinline__ void karras_node(const Key *__restrict__ codes, uint32_t n, uint32_t i,
+                                            uint4 *__restrict__ links, uint32_t *__restrict__ parents)
 {
     int l, r, ls, rs;
-    if (!karras_split(codes, (int)n, (int)i, l, r, ls, rs, max_len)) return false;
+    karras_split(codes, (int)n, (int)i, l, r, ls, rs);
     const uint32_t inner = n - 1;
     uint32_t llink = (uint32_t)l < inner ? (uint32_t)l : make_leaf((uint32_t)l - inner, 1u);
     uint32_t rlink = (uint32_t)r < inner ? (uint32_t)r : make_leaf((uint32_t)r - inner, 1u);
     links[i] = make_uint4(llink, rlink, (uint32_t)ls, (uint32_t)rs);
     parents[l] = (i << 1) | 0u;
     parents[r] = (i << 1) | 1u;
-    return true;
 }
 
 // the Morton-ordered record of one triangle (count 1 until the refit
