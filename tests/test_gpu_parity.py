@@ -184,6 +184,31 @@ def test_sort_skewed_digits_give_the_oracle_tree(kind, digit_bits, bits):
     assert_build_equals(bvh, codes, lb.ids, lb.nodes)
 
 
+@pytest.mark.parametrize("kind", ["clump", "ramp"])
+@pytest.mark.parametrize("mode", ["cis", "dis", "shadow_cis"])
+def test_trace_through_collapsed_leaves_of_many_triangles(kind, mode):
+    """Leaves collapsed from equal codes hold up to ~100,000 triangles here,
+    far past the 64 a link's count field holds, so the traversal reads their
+    count from the triangle record: rays aimed at the clumps (and some that
+    miss) give the oracle's hits and per-ray counts."""
+    tris = _skewed_scene(kind, 100_003, seed={"clump": 1, "ramp": 3}[kind])
+    lb = O.lbvh_build(tris, 30)
+    srt = O.permute(tris, lb.ids)
+    rng = np.random.default_rng(11)
+    pos = np.asarray(tris[:, :9], np.float32).reshape(-1, 3, 3)
+    tgt = pos[rng.integers(0, pos.shape[0], 1024)].mean(axis=1)
+    o = (tgt + rng.normal(0, 2.0, (1024, 3))).astype(np.float32)
+    d = (tgt - o + rng.normal(0, 0.05, (1024, 3))).astype(np.float32)
+    m = np.full(1024, S.FLT_MAX, np.float32)
+    ref, st_ref, overflow = O.trace(lb.nodes, srt, o, d, m, ORC[mode], 64, stats=True)
+    assert not overflow
+    bvh = gpu_build(tris, 30)
+    got, st = gpu_trace(bvh, o, d, m, MODES[mode], stats=True)
+    assert_hits_equal(got, ref)
+    np.testing.assert_array_equal(st, st_ref)
+    assert (got["t"] != np.float32(S.FLT_MAX)).mean() > 0.2
+
+
 def test_rebuild_reuses_buffers_and_matches():
     """Rebuilding with a second, smaller scene through the same constructor
     (the -R path, rta/main.cpp:389-400) gives that scene's tree."""
