@@ -24,8 +24,9 @@ constexpr int kSortThreads = 256;      // 8 warps
 constexpr int kSortItems = RTA_SORT_ITEMS;   // keys per thread
 // blocks per SM the onesweep kernel must fit in registers.  With the
 // lane-mask ranking, 2 (no spills) measured faster than 3 (80 registers,
-// 56-120 spilled bytes): 1M 30-bit build 0.249 -> 0.234 ms, 4M 63-bit
-// 0.996 -> 0.980 ms; 12, 24 or 32 keys per thread were not faster
+// spills): 1M 30-bit build 0.214 against 0.224 ms, 4M 63-bit 0.866 against
+// 0.891 ms (the two timed in alternating order); 12, 24 or 32 keys per
+// thread were not faster
 #ifndef RTA_SORT_MIN_BLOCKS
 #define RTA_SORT_MIN_BLOCKS 2
 #endif
