@@ -17,7 +17,13 @@ namespace rta {
 
 constexpr int kTriFloats = 26;         // cuda::simple_triangle = 104 bytes
 constexpr int kBoundsThreads = 256;
-constexpr int kSortThreads = 256;      // 8 warps
+// 8 warps of 16 keys: 512 threads of 8 or 16 keys and 1024 of 4 measured
+// slower at 4M 63-bit (0.845, 0.856, 0.933 against 0.832 ms), 256 of 8 at 3
+// or 4 blocks per SM too (0.895, 0.881 ms)
+#ifndef RTA_SORT_THREADS
+#define RTA_SORT_THREADS 256
+#endif
+constexpr int kSortThreads = RTA_SORT_THREADS;
 #ifndef RTA_SORT_ITEMS
 #define RTA_SORT_ITEMS 16
 #endif
@@ -528,9 +534,10 @@ __device__ __forceinline__ TriRec make_tri(const float *__restrict__ src, uint32
 //                of the leaf boxes; writes the record of each inner node
 //                whose range lies in the segment (a mesh's root also into its
 //                root record), the box of each leaf and such node whose
-//                parent crosses a border into that parent's record, per-leaf
-//                prefix / suffix unions and the segment union, and lists the
-//                inner nodes whose range crosses a segment border;
+//                parent crosses a border into that parent's record, the
+//                segment union, and lists the inner nodes whose range crosses
+//                a segment border, each with the union of its range's part in
+//                this segment (a suffix at l or a prefix at r);
 //   k_refit_top  the same tables over the segment unions in 256-entry groups,
 //                and in the last block a full sparse table over the groups;
 //   k_refit_ext  each listed node: its links, and its box = suffix of its
@@ -776,9 +783,9 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
     T.build(b);
     bool crosses = false;
     if (j < n_all) {
-        gstore(pre, j, T.query(0u, t));
-        gstore(suf, j, T.query(t, cnt - 1u));
         if (t == 0u) gstore(seg, blockIdx.x, T.query(0u, cnt - 1u));
+        // the mesh's last leaf: the prefix a crossing node ending there reads
+        if (jl + 1u == sp.n && sp.n > 1u) gstore(pre, j, T.query(0u, t));
         if (sp.n == 1u) {   // a one-triangle mesh: its root is the leaf
             RootRec &R = roots[sp.m];
             for (int a = 0; a < 3; ++a) {
@@ -812,7 +819,17 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
                         write_slot(nodes + sp.node_off + (node_pl >> 1), node_pl & 1u, x.lo, x.hi);
                     }
                 } else {
+                    // The node's own end j: its part within this segment.  The
+                    // largest node whose range starts at leaf l > 0 is inner
+                    // node l (Karras: the right child of the split between
+                    // l - 1 and l is leaf or inner node l), and the largest
+                    // ending at r < n - 1 is inner node r, so every crossing
+                    // node's suffix suf[l] and prefix pre[r] are written here by
+                    // nodes l and r (pre[n - 1] above); the other leaves need
+                    // neither.
                     crosses = true;
+                    if (gl == j) gstore(suf, j, T.query(t, cnt - 1u));
+                    else gstore(pre, j, T.query(0u, t));
                 }
             }
         }
