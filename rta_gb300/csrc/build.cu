@@ -157,8 +157,17 @@ k_bounds(const float *__restrict__ tris, uint32_t n, float *__restrict__ cent,
 
 // codes of every triangle plus the digit histograms of all `passes` sort
 // passes (digit width dbits) in dynamic shared memory, folded once per block
+// 1024-thread blocks, two per SM: fewer blocks fold fewer shared histograms
+// into the global ones (1M 30-bit build 0.2055 -> 0.2034 ms; 256 threads at
+// 2, 4 or 8 blocks per SM, 512 at 2 and 1024 at 1 were slower or level)
+#ifndef RTA_MORTON_THREADS
+#define RTA_MORTON_THREADS 1024
+#endif
+#ifndef RTA_MORTON_BLOCKS_PER_SM
+#define RTA_MORTON_BLOCKS_PER_SM 2
+#endif
 template <typename Key>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(RTA_MORTON_THREADS)
 k_morton(const float *__restrict__ cent, uint32_t n, Key *__restrict__ keys,
          const BuildState *__restrict__ st, SortScratchHeader *__restrict__ hdr,
          uint32_t *__restrict__ flags, int passes, int dbits, uint32_t grid_mask)
@@ -471,7 +480,8 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
     if ((rc = check_launch("k_bounds"))) return rc;
     if ((rc = mark(1))) return rc;
     const int eb = (int)((n + 255) / 256);
-    const int mb = eb < num_sms() * 8 ? eb : num_sms() * 8;
+    const int mt = RTA_MORTON_THREADS, mcap = num_sms() * RTA_MORTON_BLOCKS_PER_SM;
+    const int mb = (int)((n + mt - 1) / mt) < mcap ? (int)((n + mt - 1) / mt) : mcap;
     const uint32_t gmask = bits == 63 ? 0x1fffffu : 0x3ffu;
     const size_t hsmem = ((size_t)passes << db) * 4;
     static bool hist_smem_set = false;
@@ -482,10 +492,10 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
                                           48 * 1024));
         hist_smem_set = true;
     }
-    RTA_CUDA_TRY(bits == 63 ? launch_pdl(true, k_morton<uint64_t>, dim3(mb), dim3(256), hsmem, s,
+    RTA_CUDA_TRY(bits == 63 ? launch_pdl(true, k_morton<uint64_t>, dim3(mb), dim3(mt), hsmem, s,
                                          (const float *)c->cent, n, (uint64_t *)c->keys0,
                                          (const BuildState *)c->state, hdr, c->status, passes, db, gmask)
-                            : launch_pdl(true, k_morton<uint32_t>, dim3(mb), dim3(256), hsmem, s,
+                            : launch_pdl(true, k_morton<uint32_t>, dim3(mb), dim3(mt), hsmem, s,
                                          (const float *)c->cent, n, (uint32_t *)c->keys0,
                                          (const BuildState *)c->state, hdr, c->status, passes, db, gmask));
 
