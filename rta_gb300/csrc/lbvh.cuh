@@ -555,7 +555,7 @@ __device__ __forceinline__ void write_slot(NodeRec *nd, uint32_t side, const flo
     }
 }
 
-// 256-leaf segments (48 KB tables, 4 blocks per SM); 128 measured slower
+// 256-leaf segments; 128 measured slower
 // (more nodes cross segments: 1M build 0.270 against 0.261 ms)
 #ifndef RTA_REFIT_SEG_LOG2
 #define RTA_REFIT_SEG_LOG2 8
@@ -616,7 +616,24 @@ __device__ __forceinline__ void gstore(float *base, size_t i, const Box6 &x)
 
 __device__ __forceinline__ int floor_log2(uint32_t v) { return 31 - __clz(v); }
 
-// the sparse table of one segment in shared memory: level k, component c, entry i
+// The leaf tables of k_refit_seg keep levels 0 .. kSegLevels - 1 (windows
+// up to 16 leaves, 30 KB); a longer range joins several top windows.  Six
+// blocks per SM (40 registers) leave 60 KB of L1 for the gathers.  Measured
+// against all 8 levels at 4 blocks (48 KB): 1M 30-bit build 0.203 -> 0.197
+// ms, 4M 63-bit 0.832 -> 0.802 ms.  Tables of 6 or 7 levels at 6 or 5 blocks
+// (over 200 KB of shared memory, 28 KB of L1) measured 0.91-0.93 ms; 4 levels
+// at 6 blocks 0.807 ms; 5 or 4 levels at 7 blocks spill (0.95 ms).
+#ifndef RTA_REFIT_SEG_LEVELS
+#define RTA_REFIT_SEG_LEVELS 5
+#endif
+constexpr int kSegLevels = RTA_REFIT_SEG_LEVELS;
+#ifndef RTA_REFIT_MIN_BLOCKS
+#define RTA_REFIT_MIN_BLOCKS 6
+#endif
+
+// the sparse table of one segment in shared memory: level k, component c,
+// entry i; LEVELS levels (windows of 1 .. 2^(LEVELS - 1) entries)
+template <int LEVELS>
 struct SegTable {
     float (*t)[6][kRefitSeg];
     __device__ __forceinline__ Box6 get(int k, uint32_t i) const
@@ -628,11 +645,19 @@ struct SegTable {
         t[k][0][i] = x.lo[0]; t[k][1][i] = x.lo[1]; t[k][2][i] = x.lo[2];
         t[k][3][i] = x.hi[0]; t[k][4][i] = x.hi[1]; t[k][5][i] = x.hi[2];
     }
-    // union over entries [a, b] of the segment (two overlapping windows)
+    // union over entries [a, b] of the segment: two overlapping windows, or
+    // top windows from a on and one ending at b (joined left to right)
     __device__ __forceinline__ Box6 query(uint32_t a, uint32_t b) const
     {
-        const int k = min(floor_log2(b - a + 1u), kRefitLevels - 1);
-        return box_join(get(k, a), get(k, b + 1u - (1u << k)));
+        const uint32_t len = b - a + 1u;
+        if (LEVELS >= kRefitLevels || len <= (2u << (LEVELS - 1))) {
+            const int k = min(floor_log2(len), LEVELS - 1);
+            return box_join(get(k, a), get(k, b + 1u - (1u << k)));
+        }
+        constexpr uint32_t W = 1u << (LEVELS - 1);
+        Box6 x = get(LEVELS - 1, a);
+        for (uint32_t s = a + W; s + W - 1u < b; s += W) x = box_join(x, get(LEVELS - 1, s));
+        return box_join(x, get(LEVELS - 1, b + 1u - W));
     }
     // level 0 holds one box per thread; levels 1..7 follow
     __device__ __forceinline__ void build(const Box6 &x)
@@ -641,7 +666,7 @@ struct SegTable {
         put(0, t_, x);
         __syncthreads();
 #pragma unroll 1
-        for (int k = 1; k < kRefitLevels; ++k) {
+        for (int k = 1; k < LEVELS; ++k) {
             const uint32_t half = 1u << (k - 1);
             Box6 y = get(k - 1, t_);
             if (t_ + half < kRefitSeg) y = box_join(y, get(k - 1, t_ + half));
@@ -744,7 +769,7 @@ __device__ __forceinline__ void write_record(NodeRec *nd, const Box6 &L, const B
 namespace {
 
 template <typename Key, bool BATCH>
-__global__ void __launch_bounds__(kRefitSeg)
+__global__ void __launch_bounds__(kRefitSeg, RTA_REFIT_MIN_BLOCKS)
 k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__restrict__ meshes,
             const uint64_t *__restrict__ keys, const float *__restrict__ tris_in, uint32_t *__restrict__ ids,
             NodeRec *__restrict__ nodes, const uint4 *__restrict__ links, const uint32_t *__restrict__ parents,
@@ -753,8 +778,8 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
             uint32_t *__restrict__ n_cross, uint32_t *__restrict__ flags)
 {
     pdl_enter();
-    __shared__ float s_t[kRefitLevels][6][kRefitSeg];
-    SegTable T{s_t};
+    __shared__ float s_t[kSegLevels][6][kRefitSeg];
+    SegTable<kSegLevels> T{s_t};
     const uint32_t t = threadIdx.x, base = blockIdx.x * kRefitSeg, j = base + t;
     const uint32_t cnt = min(kRefitSeg, n_all - base);
     Box6 b{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
@@ -856,7 +881,7 @@ __device__ __forceinline__ void refit_group(float *__restrict__ t1, uint32_t nse
                                             uint32_t ngrp, int levels2, uint32_t g, uint32_t *__restrict__ ticket,
                                             float (*s_t)[6][kRefitSeg])
 {
-    SegTable T{s_t};
+    SegTable<kRefitLevels> T{s_t};
     const uint32_t t = threadIdx.x, base = g * kRefitSeg, i = base + t;
     const uint32_t cnt = min(kRefitSeg, nseg - base);
     Box6 b{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
