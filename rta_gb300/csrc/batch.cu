@@ -111,14 +111,14 @@ k_batch_bounds(const float *__restrict__ tris, uint32_t n, const uint32_t *__res
 
 // keys = mesh << 30 | 30-bit code over the mesh's box, and the digit
 // histograms of every sort pass
+template <int DBITS>
 __global__ void __launch_bounds__(256)
 k_batch_morton(const float *__restrict__ cent, uint32_t n, const uint32_t *__restrict__ tri_off,
                uint32_t meshes, const BoxKeys *__restrict__ box, uint64_t *__restrict__ keys,
-               SortScratchHeader *__restrict__ hdr, uint32_t *__restrict__ flags, int passes, int dbits)
+               SortScratchHeader *__restrict__ hdr, uint32_t *__restrict__ flags, int passes)
 {
     extern __shared__ uint32_t s_hist[];
-    const int radix = 1 << dbits;
-    const uint32_t dmask = (uint32_t)radix - 1u;
+    constexpr int radix = 1 << DBITS;
     for (int j = threadIdx.x; j < passes * radix; j += blockDim.x) s_hist[j] = 0;
     __syncthreads();
     bool wrapped = false, flat = false;
@@ -136,8 +136,7 @@ k_batch_morton(const float *__restrict__ cent, uint32_t n, const uint32_t *__res
         const float c[3] = {cent[(size_t)i * 3 + 0], cent[(size_t)i * 3 + 1], cent[(size_t)i * 3 + 2]};
         const uint64_t key = ((uint64_t)m << 30) | morton_code(c, lo, d, 0x3ffu, wrapped);
         keys[i] = key;
-        for (int p = 0; p < passes; ++p)
-            atomicAdd(&s_hist[p * radix + ((uint32_t)(key >> (dbits * p)) & dmask)], 1u);
+        hist_add<DBITS>(s_hist, key, passes);
     }
     if (__any_sync(0xffffffffu, wrapped) && (threadIdx.x & 31) == 0) atomicOr(flags, RTA_DEV_QUANT_WRAP);
     if (__any_sync(0xffffffffu, flat) && (threadIdx.x & 31) == 0) atomicOr(flags, RTA_DEV_ZERO_EXTENT);
@@ -270,8 +269,26 @@ static int batch_build_impl(rta_batch *b, const void *tris, cudaStream_t s)
     const uint32_t grid = std::min<uint32_t>(eb, (uint32_t)batch_sms() * 8u);
     k_batch_bounds<<<grid, 256, 0, s>>>(tin, n, b->tri_off_d, b->meshes, b->cent, b->box);
     if ((rc = check_launch("k_batch_bounds"))) return rc;
-    k_batch_morton<<<grid, 256, ((size_t)passes << db) * 4, s>>>(b->cent, n, b->tri_off_d, b->meshes, b->box,
-                                                                b->keys0, hdr, b->status, passes, db);
+    {
+        const size_t hs = ((size_t)passes << db) * 4;
+        switch (db) {
+        case 9:
+            k_batch_morton<9><<<grid, 256, hs, s>>>(b->cent, n, b->tri_off_d, b->meshes, b->box, b->keys0, hdr,
+                                                    b->status, passes);
+            break;
+        case 10:
+            k_batch_morton<10><<<grid, 256, hs, s>>>(b->cent, n, b->tri_off_d, b->meshes, b->box, b->keys0, hdr,
+                                                     b->status, passes);
+            break;
+        case 11:
+            k_batch_morton<11><<<grid, 256, hs, s>>>(b->cent, n, b->tri_off_d, b->meshes, b->box, b->keys0, hdr,
+                                                     b->status, passes);
+            break;
+        default:
+            k_batch_morton<8><<<grid, 256, hs, s>>>(b->cent, n, b->tri_off_d, b->meshes, b->box, b->keys0, hdr,
+                                                    b->status, passes);
+        }
+    }
     if ((rc = check_launch("k_batch_morton"))) return rc;
     uint64_t *ks = nullptr;
     uint32_t *vs = nullptr;

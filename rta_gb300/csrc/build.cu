@@ -166,16 +166,15 @@ k_bounds(const float *__restrict__ tris, uint32_t n, float *__restrict__ cent,
 #ifndef RTA_MORTON_BLOCKS_PER_SM
 #define RTA_MORTON_BLOCKS_PER_SM 2
 #endif
-template <typename Key>
+template <typename Key, int DBITS>
 __global__ void __launch_bounds__(RTA_MORTON_THREADS)
 k_morton(const float *__restrict__ cent, uint32_t n, Key *__restrict__ keys,
          const BuildState *__restrict__ st, SortScratchHeader *__restrict__ hdr,
-         uint32_t *__restrict__ flags, int passes, int dbits, uint32_t grid_mask)
+         uint32_t *__restrict__ flags, int passes, uint32_t grid_mask)
 {
     pdl_enter();
     extern __shared__ uint32_t s_hist[];
-    const int radix = 1 << dbits;
-    const uint32_t dmask = (uint32_t)radix - 1u;
+    constexpr int radix = 1 << DBITS;
     for (int j = threadIdx.x; j < passes * radix; j += blockDim.x) s_hist[j] = 0;
     __syncthreads();
     const float lo[3] = {st->lo[0], st->lo[1], st->lo[2]};
@@ -187,13 +186,42 @@ k_morton(const float *__restrict__ cent, uint32_t n, Key *__restrict__ keys,
         const float c[3] = {cent[(size_t)i * 3 + 0], cent[(size_t)i * 3 + 1], cent[(size_t)i * 3 + 2]};
         Key k = (Key)morton_code(c, lo, d, grid_mask, wrapped);
         keys[i] = k;
-        for (int p = 0; p < passes; ++p)
-            atomicAdd(&s_hist[p * radix + ((uint32_t)(k >> (dbits * p)) & dmask)], 1u);
+        hist_add<DBITS>(s_hist, k, passes);
     }
     if (__any_sync(0xffffffffu, wrapped) && (threadIdx.x & 31) == 0) atomicOr(flags, RTA_DEV_QUANT_WRAP);
     __syncthreads();
     for (int j = threadIdx.x; j < passes * radix; j += blockDim.x)
         if (s_hist[j]) atomicAdd(hdr->hist + j, s_hist[j]);
+}
+
+template <typename Key, int DBITS>
+static cudaError_t morton_launch_db(int mb, int mt, size_t hsmem, cudaStream_t s, const float *cent, uint32_t n,
+                                    void *keys, const BuildState *st, SortScratchHeader *hdr, uint32_t *flags,
+                                    int passes, uint32_t gmask)
+{
+    static bool smem_set = false;
+    if (!smem_set) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_morton<Key, DBITS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 48 * 1024);
+        if (e != cudaSuccess) return e;
+        smem_set = true;
+    }
+    return launch_pdl(true, k_morton<Key, DBITS>, dim3(mb), dim3(mt), hsmem, s, cent, n, (Key *)keys, st, hdr, flags,
+                      passes, gmask);
+}
+
+// the Morton kernel for digit width db (8 to 11)
+template <typename Key>
+static cudaError_t morton_launch(int db, int mb, int mt, size_t hsmem, cudaStream_t s, const float *cent,
+                                 uint32_t n, void *keys, const BuildState *st, SortScratchHeader *hdr,
+                                 uint32_t *flags, int passes, uint32_t gmask)
+{
+    switch (db) {
+    case 9: return morton_launch_db<Key, 9>(mb, mt, hsmem, s, cent, n, keys, st, hdr, flags, passes, gmask);
+    case 10: return morton_launch_db<Key, 10>(mb, mt, hsmem, s, cent, n, keys, st, hdr, flags, passes, gmask);
+    case 11: return morton_launch_db<Key, 11>(mb, mt, hsmem, s, cent, n, keys, st, hdr, flags, passes, gmask);
+    default: return morton_launch_db<Key, 8>(mb, mt, hsmem, s, cent, n, keys, st, hdr, flags, passes, gmask);
+    }
 }
 
 // ------------------------------------------------------------------------- //
@@ -484,20 +512,10 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
     const int mb = (int)((n + mt - 1) / mt) < mcap ? (int)((n + mt - 1) / mt) : mcap;
     const uint32_t gmask = bits == 63 ? 0x1fffffu : 0x3ffu;
     const size_t hsmem = ((size_t)passes << db) * 4;
-    static bool hist_smem_set = false;
-    if (!hist_smem_set) {
-        RTA_CUDA_TRY(cudaFuncSetAttribute(k_morton<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          48 * 1024));
-        RTA_CUDA_TRY(cudaFuncSetAttribute(k_morton<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          48 * 1024));
-        hist_smem_set = true;
-    }
-    RTA_CUDA_TRY(bits == 63 ? launch_pdl(true, k_morton<uint64_t>, dim3(mb), dim3(mt), hsmem, s,
-                                         (const float *)c->cent, n, (uint64_t *)c->keys0,
-                                         (const BuildState *)c->state, hdr, c->status, passes, db, gmask)
-                            : launch_pdl(true, k_morton<uint32_t>, dim3(mb), dim3(mt), hsmem, s,
-                                         (const float *)c->cent, n, (uint32_t *)c->keys0,
-                                         (const BuildState *)c->state, hdr, c->status, passes, db, gmask));
+    RTA_CUDA_TRY(bits == 63 ? morton_launch<uint64_t>(db, mb, mt, hsmem, s, c->cent, n, c->keys0, c->state, hdr,
+                                                      c->status, passes, gmask)
+                            : morton_launch<uint32_t>(db, mb, mt, hsmem, s, c->cent, n, c->keys0, c->state, hdr,
+                                                      c->status, passes, gmask));
 
     if ((rc = mark(2))) return rc;
     rc = bits == 63 ? sort_keys<uint64_t>(c, n, passes, hdr, tstat, s)

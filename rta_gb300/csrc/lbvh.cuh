@@ -93,16 +93,22 @@ __device__ __forceinline__ uint32_t f2u_rz_sat(float v)
     return __float2uint_rz(v);
 }
 
-// bit k of the low 21 bits of v moves to bit 3k
-__device__ __forceinline__ uint64_t spread3(uint64_t v)
+// bit k of the low 11 bits of v moves to bit 3k (in 32-bit words)
+__device__ __forceinline__ uint32_t spread3_11(uint32_t v)
 {
-    v &= 0x1fffffull;
-    v = (v | (v << 32)) & 0x001f00000000ffffull;
-    v = (v | (v << 16)) & 0x001f0000ff0000ffull;
-    v = (v | (v << 8)) & 0x100f00f00f00f00full;
-    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
-    v = (v | (v << 2)) & 0x1249249249249249ull;
+    v &= 0x7ffu;
+    v = (v | (v << 16)) & 0xff0000ffu;
+    v = (v | (v << 8)) & 0x0f00f00fu;
+    v = (v | (v << 4)) & 0xc30c30c3u;
+    v = (v | (v << 2)) & 0x49249249u;
     return v;
+}
+
+// bit k of the low 21 bits of v moves to bit 3k: bits 0..10 and 11..20 spread
+// in 32-bit words (the upper part lands at bit 33)
+__device__ __forceinline__ uint64_t spread3(uint32_t v)
+{
+    return (uint64_t)spread3_11(v) | ((uint64_t)spread3_11((v >> 11) & 0x3ffu) << 33);
 }
 
 // morton_codes2 (lbvh-kernels.cu:174-180): (center - min) * d, to unsigned,
@@ -115,6 +121,18 @@ __device__ __forceinline__ uint64_t morton_code(const float c[3], const float lo
     uint32_t z = f2u_rz_sat(__fmul_rn(__fsub_rn(c[2], lo[2]), d[2]));
     wrapped |= (x > grid_mask) | (y > grid_mask) | (z > grid_mask);
     return spread3(x & grid_mask) | (spread3(y & grid_mask) << 1) | (spread3(z & grid_mask) << 2);
+}
+
+// one key's digits of sort passes [0, passes) into shared histograms (pass
+// p's at hist + p * 2^DBITS); the digit shifts are constants
+template <int DBITS, typename Key>
+__device__ __forceinline__ void hist_add(uint32_t *hist, Key key, int passes)
+{
+    constexpr uint32_t kMask = (1u << DBITS) - 1u;
+#pragma unroll
+    for (int p = 0; p < kMaxPasses; ++p)
+        if (DBITS * p < 64 && p < passes)
+            atomicAdd(&hist[(p << DBITS) + ((uint32_t)((uint64_t)key >> (DBITS * p)) & kMask)], 1u);
 }
 
 // ------------------------------------------------------------------------- //
