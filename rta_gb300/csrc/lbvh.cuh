@@ -451,6 +451,37 @@ __device__ __forceinline__ int cpl(const Key *__restrict__ codes, int n, int i, 
     return x == 0 ? c + __clz(i ^ j) : c;
 }
 
+// The searches below only ask whether cpl(base, j) > c for a fixed c: with
+// x = codes[base] ^ codes[j], that is x < 2^(W-1-c) for c < W (key width W,
+// equal codes included), x == 0 and base ^ j < 2^(W+31-c) for c >= W (the
+// index tie-break), and true for c = -1 (codes use at most W - 1 bits) --
+// a compare instead of the leading-zero counts.
+template <typename Key>
+__device__ __forceinline__ void prefix_threshold(int c, Key &th, uint32_t &tl)
+{
+    constexpr int W = KeyBits<Key>::tie;
+    if (c < 0) {
+        th = ~(Key)0;
+        tl = 0u;
+    } else if (c < W) {
+        th = (Key)1 << (W - 1 - c);
+        tl = 0u;
+    } else {
+        th = 0;
+        tl = 1u << (W + 31 - c);
+    }
+}
+
+// cpl(base, j) > c, c given by its threshold (th, tl); false out of range
+template <typename Key>
+__device__ __forceinline__ bool longer_prefix(const Key *__restrict__ codes, int n, int base, int j, Key kb, Key th,
+                                              uint32_t tl)
+{
+    if ((unsigned)j >= (unsigned)n) return false;
+    const Key x = kb ^ __ldg(codes + j);
+    return x < th || (x == th && (uint32_t)(base ^ j) < tl);
+}
+
 // (Leaving the nodes whose range search passes 64 leaves to a second launch,
 // so that one warp's searches have alike trip counts, measured no faster:
 // the serialised passes went 29 -> 41 us at 1M and 105 -> 112 us at 4M.)
@@ -461,21 +492,23 @@ __device__ __forceinline__ void karras_split(const Key *__restrict__ codes, int 
     // build_tree_karras (:205-249): direction, range end (exponential +
     // binary search), split (binary search with ceiling halving)
     const Key ki = __ldg(codes + i);
-    int dd = cpl(codes, n, i, i + 1, ki) - cpl(codes, n, i, i - 1, ki);
-    int d = dd >= 0 ? 1 : -1;
-    int cpl_min = cpl(codes, n, i, i - d, ki);
+    const int c_next = cpl(codes, n, i, i + 1, ki), c_prev = cpl(codes, n, i, i - 1, ki);
+    const int d = c_next - c_prev >= 0 ? 1 : -1;
+    Key th;
+    uint32_t tl;
+    prefix_threshold(d > 0 ? c_prev : c_next, th, tl);   // cpl_min = cpl(i, i - d)
     int l_max = 2;
-    while (cpl(codes, n, i, i + l_max * d, ki) > cpl_min) l_max *= 2;
+    while (longer_prefix(codes, n, i, i + l_max * d, ki, th, tl)) l_max *= 2;
     int l = 0;
     for (int t = l_max / 2; t >= 1; t /= 2)
-        if (cpl(codes, n, i, i + (l + t) * d, ki) > cpl_min) l += t;
+        if (longer_prefix(codes, n, i, i + (l + t) * d, ki, th, tl)) l += t;
     int j = i + l * d;
     int from = min(i, j), to = max(i, j);
     const Key kf = __ldg(codes + from);
-    int cpl_node = cpl(codes, n, from, to, kf);
+    prefix_threshold(cpl(codes, n, from, to, kf), th, tl);   // cpl_node
     int s = 0;
     for (int t = (l + 1) / 2; t >= 1; t = (t + 1) / 2) {
-        if (cpl(codes, n, from, from + s + t, kf) > cpl_node) s += t;
+        if (longer_prefix(codes, n, from, from + s + t, kf, th, tl)) s += t;
         if (t <= 1) break;
     }
     int mid = from + s;
