@@ -73,7 +73,9 @@ typedef struct rta_lbvh {
     const void *tris;        /* n Morton-ordered triangles, 48 bytes each */
     const uint32_t *index;   /* n: Morton position -> input triangle id (lbvh.h:20-28) */
     const void *codes;       /* n sorted Morton codes: uint32 (30-bit) or uint64 (63-bit) */
-    const uint32_t *parents; /* 2n-1 parent links ((parent << 1) | side), reference numbering */
+    const uint32_t *parents; /* 2n-1 parent links ((parent << 1) | side), reference numbering;
+                                bit 31 set when the parent's Morton range crosses a
+                                256-leaf border (build bookkeeping: mask it off) */
     uint32_t n;
     int32_t morton_bits;
     uint32_t *status;        /* device word of RTA_DEV_* flags */

@@ -155,7 +155,7 @@ k_batch_karras(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ c
     const MeshRec mr = meshes[(uint32_t)(keys[i] >> 30)];
     const uint32_t li = i - mr.tri_off;
     if (li + 1 < mr.n_tris)
-        karras_node(codes + mr.tri_off, mr.n_tris, li, links + mr.node_off, parents + mr.parent_off);
+        karras_node(codes + mr.tri_off, mr.n_tris, li, links + mr.node_off, parents + mr.parent_off, mr.tri_off);
     // the Morton-ordered triangles and mesh-local ids are the refit's (k_refit_seg)
 }
 

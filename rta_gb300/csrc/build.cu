@@ -262,7 +262,7 @@ __global__ void k_to_2f4(const NodeRec *__restrict__ nodes, const RootRec *__res
     if (k >= 2 * n - 1) return;
     float lo[3], hi[3];
     uint32_t link;   // this node's link as seen from its parent (or the root record)
-    if (k != 0 && (parents[k] >> 1) >= n - 1) {   // only a broken build gets here
+    if (k != 0 && parent_index(parents[k]) >= n - 1) {   // only a broken build gets here
         out[2 * k + 0] = make_float4(0.f, 0.f, 0.f, 0.f);
         out[2 * k + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
@@ -272,7 +272,7 @@ __global__ void k_to_2f4(const NodeRec *__restrict__ nodes, const RootRec *__res
         link = root->link;
     } else {
         const uint32_t pl = parents[k];
-        const NodeRec *nd = nodes + (pl >> 1);
+        const NodeRec *nd = nodes + parent_index(pl);
         const float *f = reinterpret_cast<const float *>(nd);
         for (int a = 0; a < 3; ++a) {
             lo[a] = f[slot_lo(pl & 1u, a)];

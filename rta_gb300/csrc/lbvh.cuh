@@ -36,6 +36,9 @@ constexpr int kSortItems = RTA_SORT_ITEMS;   // keys per thread
 #ifndef RTA_SORT_MIN_BLOCKS
 #define RTA_SORT_MIN_BLOCKS 2
 #endif
+#ifndef RTA_SORT_RELOAD
+#define RTA_SORT_RELOAD 0
+#endif
 constexpr int kSortTile = kSortThreads * kSortItems;   // 4096 keys per tile
 constexpr int kMaxDigitBits = 11;
 constexpr int kMaxRadix = 1 << kMaxDigitBits;
@@ -253,15 +256,23 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
 #pragma unroll
     for (int j = 0; j < kDpt; ++j) gh[j] = tid * kDpt + j < kRadix ? hist[tid * kDpt + j] : 0u;
 
-    Key k[kSortItems];
-    uint32_t v[kSortItems];
+    // kReload: only the digits stay in registers through the ranking and the
+    // scans; keys and values are loaded again (cache hits) for the staging
+    constexpr bool kReload = RTA_SORT_RELOAD != 0;
+    Key k[kReload ? 1 : kSortItems];
+    uint32_t v[kReload ? 1 : kSortItems];
+    uint32_t dg[kSortItems];
     uint32_t rank[kSortItems];
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
         uint32_t idx = wbase + i * 32 + lane;
         bool ok = idx < n;
-        k[i] = ok ? kin[idx] : (Key)~(Key)0;
-        v[i] = ok ? (vin ? vin[idx] : idx) : 0u;
+        const Key kk = ok ? kin[idx] : (Key)~(Key)0;
+        dg[i] = (uint32_t)(kk >> shift) & kDigitMask;
+        if constexpr (!kReload) {
+            k[i] = kk;
+            v[i] = ok ? (vin ? vin[idx] : idx) : 0u;
+        }
     }
     // Stable rank of each key among the warp's keys of its digit, in (item,
     // lane) order: the lanes OR their bit into the digit's mask word; the
@@ -274,7 +285,7 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
     const uint32_t le_mask = lane_bit | (lane_bit - 1u);
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
-        const uint32_t d = (uint32_t)(k[i] >> shift) & kDigitMask;
+        const uint32_t d = dg[i];
         uint32_t *m = &S.u.match[w][d];
         atomicOr(m, lane_bit);
         __syncwarp();
@@ -334,11 +345,18 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
     // the tile in digit order in shared memory; meanwhile the predecessor
     // tiles get further with their prefixes
 #pragma unroll
+    for (int i = 0; i < kSortItems; ++i) rank[i] += S.digit_start[dg[i]] + S.whist[w][dg[i]];
+#pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
-        const uint32_t d = (uint32_t)(k[i] >> shift) & kDigitMask;
-        uint32_t pos = S.digit_start[d] + S.whist[w][d] + rank[i];
-        S.u.stage.keys[pos] = k[i];
-        S.u.stage.vals[pos] = v[i];
+        if constexpr (kReload) {
+            const uint32_t idx = wbase + i * 32 + lane;
+            const bool ok = idx < n;
+            S.u.stage.keys[rank[i]] = ok ? kin[idx] : (Key)~(Key)0;
+            S.u.stage.vals[rank[i]] = ok ? (vin ? vin[idx] : idx) : 0u;
+        } else {
+            S.u.stage.keys[rank[i]] = k[i];
+            S.u.stage.vals[rank[i]] = v[i];
+        }
     }
     {
         uint32_t gexcl = gexcl0;
@@ -424,6 +442,21 @@ int sort_passes_launch(Key *k0, Key *k1, uint32_t *v0, uint32_t *v1, uint32_t n,
 }
 
 } // namespace
+
+// The refit works on segments of 256 consecutive leaves; 128 measured slower
+// (more nodes cross segments: 1M build 0.270 against 0.261 ms)
+#ifndef RTA_REFIT_SEG_LOG2
+#define RTA_REFIT_SEG_LOG2 8
+#endif
+constexpr uint32_t kRefitSeg = 1u << RTA_REFIT_SEG_LOG2;   // leaves per segment = threads per block
+constexpr int kRefitLevels = RTA_REFIT_SEG_LOG2;           // sparse table levels (windows of 1 .. kRefitSeg / 2)
+
+__device__ __forceinline__ bool crosses_segment(uint32_t gl, uint32_t gr) { return gl / kRefitSeg != gr / kRefitSeg; }
+
+// A parent word is (parent << 1) | side, with kParentCrosses set when the
+// parent's Morton range crosses a segment border (the refit's bookkeeping).
+constexpr uint32_t kParentCrosses = 1u << 31;
+__device__ __forceinline__ uint32_t parent_index(uint32_t pl) { return (pl & ~kParentCrosses) >> 1; }
 
 // ------------------------------------------------------------------------- //
 // Karras radix tree                                                           //
@@ -521,10 +554,12 @@ __device__ __forceinline__ void karras_split(const Key *__restrict__ codes, int 
 // links of inner node i (i + 1 < n) of a tree over codes[0, n) -- (left
 // link, right link, left size, right size), into a compact array the refit
 // reads; the refit writes each node's whole record -- and its children's
-// parent words
+// parent words, flagged when node i's range crosses a segment border (the
+// tree's leaves start at leaf position base of the segmented sequence)
 template <typename Key>
 __device__ __forceinline__ void karras_node(const Key *__restrict__ codes, uint32_t n, uint32_t i,
-                                            uint4 *__restrict__ links, uint32_t *__restrict__ parents)
+                                            uint4 *__restrict__ links, uint32_t *__restrict__ parents,
+                                            uint32_t base = 0u)
 {
     int l, r, ls, rs;
     karras_split(codes, (int)n, (int)i, l, r, ls, rs);
@@ -532,8 +567,10 @@ __device__ __forceinline__ void karras_node(const Key *__restrict__ codes, uint3
     uint32_t llink = (uint32_t)l < inner ? (uint32_t)l : make_leaf((uint32_t)l - inner, 1u);
     uint32_t rlink = (uint32_t)r < inner ? (uint32_t)r : make_leaf((uint32_t)r - inner, 1u);
     links[i] = make_uint4(llink, rlink, (uint32_t)ls, (uint32_t)rs);
-    parents[l] = (i << 1) | 0u;
-    parents[r] = (i << 1) | 1u;
+    const uint32_t mid = (uint32_t)l < inner ? (uint32_t)l : (uint32_t)l - inner;   // the split
+    const uint32_t cross = crosses_segment(base + mid + 1u - (uint32_t)ls, base + mid + (uint32_t)rs) ? kParentCrosses : 0u;
+    parents[l] = (i << 1) | 0u | cross;
+    parents[r] = (i << 1) | 1u | cross;
 }
 
 // the Morton-ordered record of one triangle (count 1 until the refit
@@ -606,13 +643,6 @@ __device__ __forceinline__ void write_slot(NodeRec *nd, uint32_t side, const flo
     }
 }
 
-// 256-leaf segments; 128 measured slower
-// (more nodes cross segments: 1M build 0.270 against 0.261 ms)
-#ifndef RTA_REFIT_SEG_LOG2
-#define RTA_REFIT_SEG_LOG2 8
-#endif
-constexpr uint32_t kRefitSeg = 1u << RTA_REFIT_SEG_LOG2;   // leaves per segment = threads per block
-constexpr int kRefitLevels = RTA_REFIT_SEG_LOG2;           // sparse table levels (windows of 1 .. kRefitSeg / 2)
 // group unions whose full table k_refit_top builds in shared memory (two
 // levels in the segment table's space); more go level by level through L2
 constexpr uint32_t kMaxGroups = kRefitLevels * kRefitSeg / 2;
@@ -763,19 +793,15 @@ __device__ __forceinline__ MeshSpan mesh_of(uint32_t j, uint32_t n_all, const Me
     return MeshSpan{m, mr.tri_off, mr.n_tris, mr.node_off, mr.parent_off};
 }
 
-__device__ __forceinline__ bool crosses_segment(uint32_t gl, uint32_t gr) { return gl / kRefitSeg != gr / kRefitSeg; }
-
-// whether inner node p of mesh sp (local index) has a range that crosses a
-// segment border; false with the bad-link flag for an index out of range
-__device__ __forceinline__ bool node_crosses(const uint4 *__restrict__ links, const MeshSpan &sp, uint32_t p,
-                                             uint32_t *__restrict__ flags)
+// whether the parent (word pl) of a node of mesh sp has a range that crosses
+// a segment border; false with the bad-link flag for an index out of range
+__device__ __forceinline__ bool parent_crosses(uint32_t pl, const MeshSpan &sp, uint32_t *__restrict__ flags)
 {
-    uint32_t l, r;
-    if (p >= sp.n - 1u || !node_range(links[sp.node_off + p], sp.n, l, r)) {
+    if (parent_index(pl) >= sp.n - 1u) {
         atomicOr(flags, RTA_DEV_BAD_LINK);
         return false;
     }
-    return crosses_segment(sp.tri_off + l, sp.tri_off + r);
+    return (pl & kParentCrosses) != 0u;
 }
 
 // a child's link in its parent's record: an inner child whose codes are all
@@ -869,10 +895,10 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
                 R.hi[a] = b.hi[a];
             }
             R.link = make_leaf(0u, 1u);
-        } else if (node_crosses(links, sp, leaf_pl >> 1, flags)) {
+        } else if (parent_crosses(leaf_pl, sp, flags)) {
             // the leaf's box into its parent's record (a parent within one
             // segment writes its record itself)
-            write_slot(nodes + sp.node_off + (leaf_pl >> 1), leaf_pl & 1u, b.lo, b.hi);
+            write_slot(nodes + sp.node_off + parent_index(leaf_pl), leaf_pl & 1u, b.lo, b.hi);
         }
         // inner node jl of the mesh (one end of its range): its record here
         // when the range lies in this segment, else on the list for k_refit_ext
@@ -890,9 +916,9 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
                     write_record(nodes + sp.node_off + jl, bl, br, q);
                     if (jl == 0u) {
                         write_root(codes, sp, box_join(bl, br), tris, roots);
-                    } else if (node_crosses(links, sp, node_pl >> 1, flags)) {
+                    } else if (parent_crosses(node_pl, sp, flags)) {
                         const Box6 x = box_join(bl, br);
-                        write_slot(nodes + sp.node_off + (node_pl >> 1), node_pl & 1u, x.lo, x.hi);
+                        write_slot(nodes + sp.node_off + parent_index(node_pl), node_pl & 1u, x.lo, x.hi);
                     }
                 } else {
                     // The node's own end j: its part within this segment.  The
@@ -1052,7 +1078,7 @@ __device__ __forceinline__ void refit_cross(const Key *__restrict__ codes, uint3
         write_root(codes, sp, x, tris, roots);
         return;
     }
-    const uint32_t pl = parents[sp.parent_off + jl], p = pl >> 1;
+    const uint32_t pl = parents[sp.parent_off + jl], p = parent_index(pl);
     if (p >= sp.n - 1u) {
         atomicOr(flags, RTA_DEV_BAD_LINK);
         return;
