@@ -36,9 +36,6 @@ constexpr int kSortItems = RTA_SORT_ITEMS;   // keys per thread
 #ifndef RTA_SORT_MIN_BLOCKS
 #define RTA_SORT_MIN_BLOCKS 2
 #endif
-#ifndef RTA_SORT_RELOAD
-#define RTA_SORT_RELOAD 0
-#endif
 constexpr int kSortTile = kSortThreads * kSortItems;   // 4096 keys per tile
 constexpr int kMaxDigitBits = 11;
 constexpr int kMaxRadix = 1 << kMaxDigitBits;
@@ -256,24 +253,20 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
 #pragma unroll
     for (int j = 0; j < kDpt; ++j) gh[j] = tid * kDpt + j < kRadix ? hist[tid * kDpt + j] : 0u;
 
-    // kReload: only the digits stay in registers through the ranking and the
-    // scans; keys and values are loaded again (cache hits) for the staging
-    constexpr bool kReload = RTA_SORT_RELOAD != 0;
-    Key k[kReload ? 1 : kSortItems];
-    uint32_t v[kReload ? 1 : kSortItems];
-    uint32_t dg[kSortItems];
+    // (Keeping only the digits in registers through the ranking and loading
+    // keys and values again for the staging, 80 registers and three blocks
+    // per SM, measured no faster: the second load's latency ate the gain.)
+    Key k[kSortItems];
+    uint32_t v[kSortItems];
     uint32_t rank[kSortItems];
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
         uint32_t idx = wbase + i * 32 + lane;
         bool ok = idx < n;
-        const Key kk = ok ? kin[idx] : (Key)~(Key)0;
-        dg[i] = (uint32_t)(kk >> shift) & kDigitMask;
-        if constexpr (!kReload) {
-            k[i] = kk;
-            v[i] = ok ? (vin ? vin[idx] : idx) : 0u;
-        }
+        k[i] = ok ? kin[idx] : (Key)~(Key)0;
+        v[i] = ok ? (vin ? vin[idx] : idx) : 0u;
     }
+    auto digit = [&](int i) -> uint32_t { return (uint32_t)(k[i] >> shift) & kDigitMask; };
     // Stable rank of each key among the warp's keys of its digit, in (item,
     // lane) order: the lanes OR their bit into the digit's mask word; the
     // highest lane of a mask is its leader, adds the lane count to the warp's
@@ -285,7 +278,7 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
     const uint32_t le_mask = lane_bit | (lane_bit - 1u);
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
-        const uint32_t d = dg[i];
+        const uint32_t d = digit(i);
         uint32_t *m = &S.u.match[w][d];
         atomicOr(m, lane_bit);
         __syncwarp();
@@ -345,18 +338,14 @@ k_onesweep(const Key *__restrict__ kin, const uint32_t *__restrict__ vin, Key *_
     // the tile in digit order in shared memory; meanwhile the predecessor
     // tiles get further with their prefixes
 #pragma unroll
-    for (int i = 0; i < kSortItems; ++i) rank[i] += S.digit_start[dg[i]] + S.whist[w][dg[i]];
+    for (int i = 0; i < kSortItems; ++i) {
+        const uint32_t d = digit(i);
+        rank[i] += S.digit_start[d] + S.whist[w][d];
+    }
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
-        if constexpr (kReload) {
-            const uint32_t idx = wbase + i * 32 + lane;
-            const bool ok = idx < n;
-            S.u.stage.keys[rank[i]] = ok ? kin[idx] : (Key)~(Key)0;
-            S.u.stage.vals[rank[i]] = ok ? (vin ? vin[idx] : idx) : 0u;
-        } else {
-            S.u.stage.keys[rank[i]] = k[i];
-            S.u.stage.vals[rank[i]] = v[i];
-        }
+        S.u.stage.keys[rank[i]] = k[i];
+        S.u.stage.vals[rank[i]] = v[i];
     }
     {
         uint32_t gexcl = gexcl0;
