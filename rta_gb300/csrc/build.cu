@@ -160,6 +160,13 @@ k_bounds(const float *__restrict__ tris, uint32_t n, float *__restrict__ cent,
 // 1024-thread blocks, two per SM: fewer blocks fold fewer shared histograms
 // into the global ones (1M 30-bit build 0.2055 -> 0.2034 ms; 256 threads at
 // 2, 4 or 8 blocks per SM, 512 at 2 and 1024 at 1 were slower or level)
+// The Morton-ordered 48-byte triangles are gathered in the Karras kernel,
+// whose split searches are latency-bound and leave the memory system idle;
+// the refit then reads them in order.  Measured against gathering them in
+// k_refit_seg: 4M 63-bit build 0.791 -> 0.778 ms, 1M 30-bit level.
+#ifndef RTA_KARRAS_GATHER
+#define RTA_KARRAS_GATHER 1
+#endif
 #ifndef RTA_MORTON_THREADS
 #define RTA_MORTON_THREADS 1024
 #endif
@@ -232,12 +239,20 @@ template <typename Key>
 __global__ void __launch_bounds__(256)
 k_karras(const Key *__restrict__ codes, const uint32_t *__restrict__ ids, uint32_t n,
          uint4 *__restrict__ links, uint32_t *__restrict__ parents,
-         const float *__restrict__ tris_in, float *__restrict__ tris_out)
+         const float *__restrict__ tris_in, float *__restrict__ tris_out, TriRec *__restrict__ tris_rec)
 {
     pdl_enter();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    // with tris_rec: the 48-byte triangle of sorted position i (its gather
+    // overlaps the split search)
+    TriRec tr;
+    if (tris_rec) {
+        const uint32_t id = __ldg(ids + i);
+        tr = make_tri(tris_in + (size_t)id * kTriFloats, id);
+    }
     if (i + 1 < n) karras_node(codes, n, i, links, parents);
+    if (tris_rec) tris_rec[i] = tr;
     // invert_triangle_permutation_cuda (:557-578): the 104-byte records in
     // Morton order, when asked for (the 48-byte TriRecs are k_refit_seg's)
     if (tris_out) {
@@ -522,19 +537,20 @@ int rta_lbvh_build(rta_lbvh_ctx *c, const void *tris, uint32_t n, int bits, void
                     : sort_keys<uint32_t>(c, n, passes, hdr, tstat, s);
     if (rc) return rc;
     if ((rc = mark(3))) return rc;
+    TriRec *kg = RTA_KARRAS_GATHER ? c->tris : nullptr;
     RTA_CUDA_TRY(bits == 63 ? launch_pdl(true, k_karras<uint64_t>, dim3(eb), dim3(256), 0, s,
                                          (const uint64_t *)c->codes, (const uint32_t *)c->index, n, c->links,
-                                         c->parents, tin, (float *)tris_out)
+                                         c->parents, tin, (float *)tris_out, kg)
                             : launch_pdl(true, k_karras<uint32_t>, dim3(eb), dim3(256), 0, s,
                                          (const uint32_t *)c->codes, (const uint32_t *)c->index, n, c->links,
-                                         c->parents, tin, (float *)tris_out));
+                                         c->parents, tin, (float *)tris_out, kg));
     if ((rc = mark(4))) return rc;
     const uint32_t cap = n > 1 ? n - 1 : 1;
-    rc = bits == 63 ? refit_launch<uint64_t, false>((const uint64_t *)c->codes, n, nullptr, nullptr, tin, c->index,
+    rc = bits == 63 ? refit_launch<uint64_t, false>((const uint64_t *)c->codes, n, nullptr, nullptr, kg ? nullptr : tin, c->index,
                                                     c->nodes, c->links, c->parents, c->tris, c->root, c->rbox, c->counters,
                                                     cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s,
                                                     true)
-                    : refit_launch<uint32_t, false>((const uint32_t *)c->codes, n, nullptr, nullptr, tin, c->index,
+                    : refit_launch<uint32_t, false>((const uint32_t *)c->codes, n, nullptr, nullptr, kg ? nullptr : tin, c->index,
                                                     c->nodes, c->links, c->parents, c->tris, c->root, c->rbox, c->counters,
                                                     cap, &hdr->n_cross, &hdr->refit_ticket, c->status, num_sms(), s,
                                                     true);

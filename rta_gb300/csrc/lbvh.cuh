@@ -865,10 +865,15 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
         // triangle of sorted position j, in Morton order, with its id local
         // to its mesh (collapse counts land in .w after the table build's
         // barrier, or in a later kernel)
-        const uint32_t id = ids[j], lid = id - sp.tri_off;
-        const TriRec tr = make_tri(tris_in + (size_t)id * kTriFloats, lid);
-        tris[j] = tr;
-        if (BATCH) ids[j] = lid;
+        TriRec tr;
+        if (tris_in) {
+            const uint32_t id = ids[j], lid = id - sp.tri_off;
+            tr = make_tri(tris_in + (size_t)id * kTriFloats, lid);
+            tris[j] = tr;
+            if (BATCH) ids[j] = lid;
+        } else {   // gathered by the Karras kernel
+            tr = tris[j];
+        }
         b = leaf_box(tr);
     }
     T.build(b);
