@@ -445,6 +445,9 @@ __device__ __forceinline__ bool crosses_segment(uint32_t gl, uint32_t gr) { retu
 // A parent word is (parent << 1) | side, with kParentCrosses set when the
 // parent's Morton range crosses a segment border (the refit's bookkeeping).
 constexpr uint32_t kParentCrosses = 1u << 31;
+// A link record's size words (z, w) carry kCollapses when that child is an
+// inner node whose codes are all equal (it becomes a leaf of the parent).
+constexpr uint32_t kCollapses = 1u << 31;
 __device__ __forceinline__ uint32_t parent_index(uint32_t pl) { return (pl & ~kParentCrosses) >> 1; }
 
 // ------------------------------------------------------------------------- //
@@ -555,9 +558,14 @@ __device__ __forceinline__ void karras_node(const Key *__restrict__ codes, uint3
     const uint32_t inner = n - 1;
     uint32_t llink = (uint32_t)l < inner ? (uint32_t)l : make_leaf((uint32_t)l - inner, 1u);
     uint32_t rlink = (uint32_t)r < inner ? (uint32_t)r : make_leaf((uint32_t)r - inner, 1u);
-    links[i] = make_uint4(llink, rlink, (uint32_t)ls, (uint32_t)rs);
     const uint32_t mid = (uint32_t)l < inner ? (uint32_t)l : (uint32_t)l - inner;   // the split
-    const uint32_t cross = crosses_segment(base + mid + 1u - (uint32_t)ls, base + mid + (uint32_t)rs) ? kParentCrosses : 0u;
+    // an inner child whose codes are all equal collapses to a leaf: flagged
+    // in its size word for the refit
+    const uint32_t from = mid + 1u - (uint32_t)ls, to = mid + (uint32_t)rs;
+    const bool lcol = ls > 1 && __ldg(codes + from) == __ldg(codes + mid);
+    const bool rcol = rs > 1 && __ldg(codes + mid + 1u) == __ldg(codes + to);
+    links[i] = make_uint4(llink, rlink, (uint32_t)ls | (lcol ? kCollapses : 0u), (uint32_t)rs | (rcol ? kCollapses : 0u));
+    const uint32_t cross = crosses_segment(base + from, base + to) ? kParentCrosses : 0u;
     parents[l] = (i << 1) | 0u | cross;
     parents[r] = (i << 1) | 1u | cross;
 }
@@ -760,7 +768,7 @@ __device__ __forceinline__ Box6 t1_query(const float *t1, uint32_t nseg, uint32_
 __device__ __forceinline__ bool node_range(const uint4 q3, uint32_t n, uint32_t &l, uint32_t &r)
 {
     const uint32_t rf = is_leaf(q3.y) ? leaf_first(q3.y) : q3.y;   // split + 1
-    const uint32_t ls = q3.z, rs = q3.w;
+    const uint32_t ls = q3.z & ~kCollapses, rs = q3.w & ~kCollapses;
     if (rf == 0u || ls == 0u || rs == 0u || ls > rf || rs > n - rf) return false;
     l = rf - ls;
     r = rf + rs - 1u;
@@ -796,11 +804,11 @@ __device__ __forceinline__ bool parent_crosses(uint32_t pl, const MeshSpan &sp, 
 // a child's link in its parent's record: an inner child whose codes are all
 // equal collapses to a leaf of its gr - gl + 1 triangles (the triangle record
 // at gl keeps the largest such count)
-template <typename Key>
-__device__ __forceinline__ uint32_t child_link(const Key *__restrict__ codes, const MeshSpan &sp, uint32_t link,
-                                               uint32_t gl, uint32_t gr, TriRec *__restrict__ tris)
+// (the Karras kernel flagged that case in the child's size word)
+__device__ __forceinline__ uint32_t child_link(uint32_t size_word, const MeshSpan &sp, uint32_t link, uint32_t gl,
+                                               uint32_t gr, TriRec *__restrict__ tris)
 {
-    if (is_leaf(link) || codes[gl] != codes[gr]) return link;
+    if (is_leaf(link) || !(size_word & kCollapses)) return link;
     const uint32_t cnt = gr - gl + 1u;
     atomicMax(reinterpret_cast<uint32_t *>(&tris[gl].v0.w), cnt);
     return make_leaf(gl - sp.tri_off, cnt);
@@ -901,12 +909,12 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
             if (!node_range(q3, sp.n, l, r)) {
                 atomicOr(flags, RTA_DEV_BAD_LINK);
             } else {
-                const uint32_t gl = sp.tri_off + l, gr = sp.tri_off + r, gm = gl + q3.z;   // gm: right child's first
+                const uint32_t gl = sp.tri_off + l, gr = sp.tri_off + r, gm = gr + 1u - (q3.w & ~kCollapses);   // gm: right child's first
                 if (!crosses_segment(gl, gr)) {
                     const Box6 bl = T.query(gl - base, gm - 1u - base), br = T.query(gm - base, gr - base);
-                    uint4 q = q3;
-                    q.x = child_link(codes, sp, q3.x, gl, gm - 1u, tris);
-                    q.y = child_link(codes, sp, q3.y, gm, gr, tris);
+                    const uint4 q = make_uint4(child_link(q3.z, sp, q3.x, gl, gm - 1u, tris),
+                                               child_link(q3.w, sp, q3.y, gm, gr, tris), q3.z & ~kCollapses,
+                                               q3.w & ~kCollapses);
                     write_record(nodes + sp.node_off + jl, bl, br, q);
                     if (jl == 0u) {
                         write_root(codes, sp, box_join(bl, br), tris, roots);
@@ -1041,7 +1049,7 @@ __device__ __forceinline__ void refit_cross(const Key *__restrict__ codes, uint3
     if (jl + 1u >= sp.n) return;
     const uint4 q3 = links[sp.node_off + jl];
     if (!node_range(q3, sp.n, l, r)) return;
-    const uint32_t gl = sp.tri_off + l, gr = sp.tri_off + r, gm = gl + q3.z;
+    const uint32_t gl = sp.tri_off + l, gr = sp.tri_off + r, gm = gr + 1u - (q3.w & ~kCollapses);
     const uint32_t sa = gl / kRefitSeg, sb = gr / kRefitSeg;
     if (sa == sb) return;
     Box6 x = gload(suf, gl);
@@ -1063,10 +1071,9 @@ __device__ __forceinline__ void refit_cross(const Key *__restrict__ codes, uint3
     }
     x = box_join(x, gload(pre, gr));
     // the node's links (its children write their boxes into its record)
-    uint4 q = q3;
-    q.x = child_link(codes, sp, q3.x, gl, gm - 1u, tris);
-    q.y = child_link(codes, sp, q3.y, gm, gr, tris);
-    nodes[sp.node_off + jl].q3 = q;
+    nodes[sp.node_off + jl].q3 = make_uint4(child_link(q3.z, sp, q3.x, gl, gm - 1u, tris),
+                                            child_link(q3.w, sp, q3.y, gm, gr, tris), q3.z & ~kCollapses,
+                                            q3.w & ~kCollapses);
     // its box into its parent's record, whose range crosses a border too
     if (jl == 0u) {
         write_root(codes, sp, x, tris, roots);
