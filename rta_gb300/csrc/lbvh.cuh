@@ -709,19 +709,21 @@ constexpr int kSegLevels = RTA_REFIT_SEG_LEVELS;
 #define RTA_REFIT_MIN_BLOCKS 6
 #endif
 
-// the sparse table of one segment in shared memory: level k, component c,
+// the sparse table of one segment in shared memory: level k, axis c,
 // entry i; LEVELS levels (windows of 1 .. 2^(LEVELS - 1) entries)
 template <int LEVELS>
 struct SegTable {
-    float (*t)[6][kRefitSeg];
+    float2 (*t)[3][kRefitSeg];   // per level and axis: (lo, hi) of entry i
     __device__ __forceinline__ Box6 get(int k, uint32_t i) const
     {
-        return Box6{{t[k][0][i], t[k][1][i], t[k][2][i]}, {t[k][3][i], t[k][4][i], t[k][5][i]}};
+        const float2 x = t[k][0][i], y = t[k][1][i], z = t[k][2][i];
+        return Box6{{x.x, y.x, z.x}, {x.y, y.y, z.y}};
     }
-    __device__ __forceinline__ void put(int k, uint32_t i, const Box6 &x)
+    __device__ __forceinline__ void put(int k, uint32_t i, const Box6 &b)
     {
-        t[k][0][i] = x.lo[0]; t[k][1][i] = x.lo[1]; t[k][2][i] = x.lo[2];
-        t[k][3][i] = x.hi[0]; t[k][4][i] = x.hi[1]; t[k][5][i] = x.hi[2];
+        t[k][0][i] = make_float2(b.lo[0], b.hi[0]);
+        t[k][1][i] = make_float2(b.lo[1], b.hi[1]);
+        t[k][2][i] = make_float2(b.lo[2], b.hi[2]);
     }
     // union over entries [a, b] of the segment: two overlapping windows, or
     // top windows from a on and one ending at b (joined left to right)
@@ -737,16 +739,18 @@ struct SegTable {
         for (uint32_t s = a + W; s + W - 1u < b; s += W) x = box_join(x, get(LEVELS - 1, s));
         return box_join(x, get(LEVELS - 1, b + 1u - W));
     }
-    // level 0 holds one box per thread; levels 1..7 follow
+    // level 0 holds one box per thread; each level's entry joins the thread's
+    // own entry of the level below (kept in registers) with the one half a
+    // window further on
     __device__ __forceinline__ void build(const Box6 &x)
     {
         const uint32_t t_ = threadIdx.x;
-        put(0, t_, x);
+        Box6 y = x;
+        put(0, t_, y);
         __syncthreads();
 #pragma unroll 1
         for (int k = 1; k < LEVELS; ++k) {
             const uint32_t half = 1u << (k - 1);
-            Box6 y = get(k - 1, t_);
             if (t_ + half < kRefitSeg) y = box_join(y, get(k - 1, t_ + half));
             put(k, t_, y);
             __syncthreads();
@@ -852,7 +856,7 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
             uint32_t *__restrict__ n_cross, uint32_t *__restrict__ flags)
 {
     pdl_enter();
-    __shared__ float s_t[kSegLevels][6][kRefitSeg];
+    __shared__ float2 s_t[kSegLevels][3][kRefitSeg];
     SegTable<kSegLevels> T{s_t};
     const uint32_t t = threadIdx.x, base = blockIdx.x * kRefitSeg, j = base + t;
     const uint32_t cnt = min(kRefitSeg, n_all - base);
@@ -958,7 +962,7 @@ k_refit_seg(const Key *__restrict__ codes, uint32_t n_all, const MeshRec *__rest
 // 1M build 0.215 -> 0.223 ms, 4M 0.871 -> 0.896 ms.)
 __device__ __forceinline__ void refit_group(float *__restrict__ t1, uint32_t nseg, float *__restrict__ t2,
                                             uint32_t ngrp, int levels2, uint32_t g, uint32_t *__restrict__ ticket,
-                                            float (*s_t)[6][kRefitSeg])
+                                            float2 (*s_t)[3][kRefitSeg])
 {
     SegTable<kRefitLevels> T{s_t};
     const uint32_t t = threadIdx.x, base = g * kRefitSeg, i = base + t;
@@ -993,7 +997,7 @@ __device__ __forceinline__ void refit_group(float *__restrict__ t1, uint32_t nse
     }
     // the group table in this block's shared memory (two levels of up to
     // kMaxGroups entries in the segment table's space), each level stored out
-    float(*lv)[6][kMaxGroups] = reinterpret_cast<float(*)[6][kMaxGroups]>(&s_t[0][0][0]);
+    float(*lv)[6][kMaxGroups] = reinterpret_cast<float(*)[6][kMaxGroups]>(&s_t[0][0][0].x);
     for (uint32_t e = t; e < ngrp; e += kRefitSeg) {
         const Box6 y = gload_cg(t2, e);
         for (int c = 0; c < 3; ++c) {
@@ -1027,7 +1031,7 @@ k_refit_top(float *__restrict__ t1, uint32_t nseg, float *__restrict__ t2, uint3
             uint32_t *__restrict__ ticket)
 {
     pdl_enter();
-    __shared__ float s_t[kRefitLevels][6][kRefitSeg];
+    __shared__ float2 s_t[kRefitLevels][3][kRefitSeg];
     refit_group(t1, nseg, t2, ngrp, levels2, blockIdx.x, ticket, s_t);
 }
 
