@@ -145,18 +145,30 @@ k_batch_morton(const float *__restrict__ cent, uint32_t n, const uint32_t *__res
         if (s_hist[j]) atomicAdd(hdr->hist + j, s_hist[j]);
 }
 
-// every inner node of every mesh; Morton-ordered triangles; ids made local
+// every inner node of every mesh; with tris, also the Morton-ordered
+// triangles and the mesh-local ids (else the refit's, k_refit_seg)
 __global__ void __launch_bounds__(256)
 k_batch_karras(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ codes, uint32_t n,
-               const MeshRec *__restrict__ meshes, uint4 *__restrict__ links, uint32_t *__restrict__ parents)
+               const MeshRec *__restrict__ meshes, uint4 *__restrict__ links, uint32_t *__restrict__ parents,
+               const float *__restrict__ tris_in, uint32_t *__restrict__ ids, TriRec *__restrict__ tris)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const MeshRec mr = meshes[(uint32_t)(keys[i] >> 30)];
     const uint32_t li = i - mr.tri_off;
+    TriRec tr;
+    uint32_t lid = 0;
+    if (tris) {
+        const uint32_t id = __ldg(ids + i);
+        lid = id - mr.tri_off;
+        tr = make_tri(tris_in + (size_t)id * kTriFloats, lid);
+    }
     if (li + 1 < mr.n_tris)
         karras_node(codes + mr.tri_off, mr.n_tris, li, links + mr.node_off, parents + mr.parent_off, mr.tri_off);
-    // the Morton-ordered triangles and mesh-local ids are the refit's (k_refit_seg)
+    if (tris) {
+        tris[i] = tr;
+        ids[i] = lid;
+    }
 }
 
 // reset_intersections (librta/cuda-kernels.cu:24-44): t, beta, gamma; ref kept
@@ -312,10 +324,11 @@ static int batch_build_impl(rta_batch *b, const void *tris, cudaStream_t s)
     if (rc) return rc;
     b->keys_sorted = ks;
     b->index = vs;
-    k_batch_karras<<<eb, 256, 0, s>>>(ks, b->codes, n, b->meshes_d, b->links, b->parents);
+    TriRec *kg = RTA_KARRAS_GATHER ? b->tris : nullptr;
+    k_batch_karras<<<eb, 256, 0, s>>>(ks, b->codes, n, b->meshes_d, b->links, b->parents, tin, vs, kg);
     if ((rc = check_launch("k_batch_karras"))) return rc;
     const uint32_t inner = n - b->meshes;
-    rc = refit_launch<uint32_t, true>(b->codes, n, b->meshes_d, ks, tin, vs, b->nodes, b->links, b->parents, b->tris,
+    rc = refit_launch<uint32_t, true>(b->codes, n, b->meshes_d, ks, kg ? nullptr : tin, vs, b->nodes, b->links, b->parents, b->tris,
                                       b->roots, b->rbox, b->counters, inner ? inner : 1u, &hdr->n_cross, &hdr->refit_ticket,
                                       b->status, batch_sms(), s);
     if (rc) return rc;

@@ -160,13 +160,6 @@ k_bounds(const float *__restrict__ tris, uint32_t n, float *__restrict__ cent,
 // 1024-thread blocks, two per SM: fewer blocks fold fewer shared histograms
 // into the global ones (1M 30-bit build 0.2055 -> 0.2034 ms; 256 threads at
 // 2, 4 or 8 blocks per SM, 512 at 2 and 1024 at 1 were slower or level)
-// The Morton-ordered 48-byte triangles are gathered in the Karras kernel,
-// whose split searches are latency-bound and leave the memory system idle;
-// the refit then reads them in order.  Measured against gathering them in
-// k_refit_seg: 4M 63-bit build 0.791 -> 0.778 ms, 1M 30-bit level.
-#ifndef RTA_KARRAS_GATHER
-#define RTA_KARRAS_GATHER 1
-#endif
 #ifndef RTA_MORTON_THREADS
 #define RTA_MORTON_THREADS 1024
 #endif
