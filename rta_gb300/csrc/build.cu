@@ -247,7 +247,7 @@ k_karras(const Key *__restrict__ codes, const uint32_t *__restrict__ ids, uint32
     if (i + 1 < n) karras_node(codes, n, i, links, parents);
     if (tris_rec) tris_rec[i] = tr;
     // invert_triangle_permutation_cuda (:557-578): the 104-byte records in
-    // Morton order, when asked for (the 48-byte TriRecs are k_refit_seg's)
+    // Morton order, when asked for (the 48-byte triangles are gathered above)
     if (tris_out) {
         const uint32_t id = __ldg(ids + i);
         const float *src = tris_in + (size_t)id * kTriFloats;

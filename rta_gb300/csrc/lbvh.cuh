@@ -146,7 +146,7 @@ __device__ __forceinline__ void hist_add(uint32_t *hist, Key key, int passes)
 // look-back across tiles for the per-digit prefix (Merrill & Garland's
 // single-pass scan as used by Adinets & Merrill's Onesweep), a shared-memory
 // staging of the tile in digit order, and coalesced runs out to global
-// memory.  BITS is the digit width (8, 10 or 11): wider digits mean fewer
+// memory.  BITS is the digit width (8 to 11): wider digits mean fewer
 // passes but larger per-warp counters and more look-back work per tile.
 
 template <typename Key, int BITS>
@@ -1139,9 +1139,10 @@ inline RefitLayout refit_layout(uint32_t n)
     return L;
 }
 
-// The refit of n_all leaves after the Karras kernel; it also writes the
-// Morton-ordered triangles (ids[j] = input index of sorted position j;
-// rewritten local to the mesh in a batch).  Tables in rbox
+// The refit of n_all leaves after the Karras kernel.  With tris_in it also
+// gathers the Morton-ordered triangles (ids[j] = input index of sorted
+// position j; rewritten local to the mesh in a batch); with tris_in null the
+// Karras kernel has written them to tris already.  Tables in rbox
 // (refit_layout(n_all).total boxes), the crossing list in cross (one word per
 // inner node: cross_cap), *n_cross and *ticket zero on entry.
 template <typename Key, bool BATCH>
