@@ -134,6 +134,13 @@ int rta_lbvh_get(const rta_lbvh_ctx *ctx, rta_lbvh *out);
 /* Synchronises the stream and returns the device status flags (RTA_DEV_*). */
 int rta_lbvh_status(const rta_lbvh *bvh, rta_stream_t stream, uint32_t *flags);
 
+/* Self-test of the bounded waits: one small kernel runs the single-pass
+ * scans' look-back against a predecessor status word that nothing writes,
+ * so every wait gives up at its poll limit (about a second) instead of
+ * hanging.  Returns the device flags it raised in *flags (RTA_DEV_SPIN_TIMEOUT
+ * expected); the context stays usable.  Synchronises the stream. */
+int rta_selftest_bounded_wait(rta_stream_t stream, uint32_t *flags);
+
 /* Writes the tree in the reference's 2F4 node layout ((2n-1) x 32 bytes),
  * node for node as buildTreeKarras + buildBoundingBoxesKarras2 leave it, for
  * dumps (bbvh.h:36-52) and parity checks. */

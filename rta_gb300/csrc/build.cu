@@ -259,6 +259,18 @@ k_karras(const Key *__restrict__ codes, const uint32_t *__restrict__ ids, uint32
 }
 
 // ------------------------------------------------------------------------- //
+// kernel: the bounded-wait self-test                                           //
+// ------------------------------------------------------------------------- //
+
+// Tile 1's look-back for 32 counters whose tile-0 words stay zero ("not
+// written yet"): each lane polls to the limit, raises the timeout flag and
+// returns.
+__global__ void k_selftest_wait(const uint32_t *__restrict__ stat, uint32_t *__restrict__ flags)
+{
+    (void)lookback(stat + threadIdx.x, 32u, 1u, flags);
+}
+
+// ------------------------------------------------------------------------- //
 // kernel: write the reference 2F4 node array (dumps and parity checks)       //
 // ------------------------------------------------------------------------- //
 
@@ -603,6 +615,27 @@ int rta_lbvh_status(const rta_lbvh *bvh, rta_stream_t stream, uint32_t *flags)
     if (!bvh || !flags) return RTA_ERR_INVALID;
     RTA_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
     RTA_CUDA_TRY(cudaMemcpy(flags, bvh->status, 4, cudaMemcpyDeviceToHost));
+    return RTA_OK;
+}
+
+int rta_selftest_bounded_wait(rta_stream_t stream, uint32_t *flags)
+{
+    if (!flags) return RTA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t *d = nullptr;   // [0]: flags, [1 .. 32]: tile 0's status words (never written)
+    RTA_CUDA_TRY(cudaMalloc(&d, 33 * 4));
+    cudaError_t e = cudaMemsetAsync(d, 0, 33 * 4, s);
+    if (e == cudaSuccess) {
+        k_selftest_wait<<<1, 32, 0, s>>>(d + 1, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMemcpy(flags, d, 4, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "rta_selftest_bounded_wait");
+        return RTA_ERR_CUDA;
+    }
     return RTA_OK;
 }
 

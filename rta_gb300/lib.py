@@ -23,7 +23,7 @@ LBVH_PASSES = 5
 SYMBOLS = [
     "rta_last_error", "rta_lbvh_max_triangles", "rta_lbvh_create", "rta_lbvh_destroy",
     "rta_lbvh_reserve", "rta_lbvh_set_digit_bits", "rta_lbvh_build", "rta_lbvh_set_timing", "rta_lbvh_pass_ms",
-    "rta_lbvh_get", "rta_lbvh_status", "rta_lbvh_to_2f4",
+    "rta_lbvh_get", "rta_lbvh_status", "rta_selftest_bounded_wait", "rta_lbvh_to_2f4",
     "rta_trace", "rta_setup_shirley_rays", "rta_reset_intersections", "rta_frame_create",
     "rta_frame_destroy", "rta_frame_get", "rta_diffuse_bounce", "rta_frame_run",
     "rta_frame_status", "rta_frame_set_timing", "rta_frame_trace_ms", "rta_host_frames_create", "rta_host_frames_destroy", "rta_host_frames_run",
@@ -92,6 +92,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.rta_lbvh_pass_ms.argtypes = [vp, P(f32)]
     L.rta_lbvh_get.argtypes = [vp, P(LbvhView)]
     L.rta_lbvh_status.argtypes = [P(LbvhView), vp, P(u32)]
+    L.rta_selftest_bounded_wait.argtypes = [vp, P(u32)]
     L.rta_lbvh_to_2f4.argtypes = [P(LbvhView), vp, vp]
     L.rta_trace.argtypes = [P(LbvhView), vp, vp, vp, u32, vp, vp, u32, vp, vp]
     L.rta_setup_shirley_rays.argtypes = [vp, vp, vp, f32, f32, i32, i32, vp, vp, vp, f32, vp]

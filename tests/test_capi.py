@@ -63,6 +63,7 @@ def test_invalid_arguments_are_rejected_without_a_device(lib):
     assert lib.rta_setup_shirley_rays(None, None, None, 0.5, 1.0, 0, 0, None, None, None, 1.0,
                                       None) == L.ERR_INVALID
     assert lib.rta_frame_create(None, 10) == L.ERR_INVALID
+    assert lib.rta_selftest_bounded_wait(None, None) == L.ERR_INVALID
 
 
 def test_max_triangles_matches_link_encoding(lib):
